@@ -1,0 +1,136 @@
+"""ctypes binding of the CPU restatement (test infrastructure only).
+
+Only the tests, the smoke check and the CPU-baseline leg of bench.py use this
+module, as the checker.  The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+FAITHFUL, GPU = 0, 1
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("ni", ctypes.c_int), ("nj", ctypes.c_int),
+                ("re", ctypes.c_double), ("pr", ctypes.c_double), ("dt", ctypes.c_double),
+                ("vel_rot", ctypes.c_double), ("uin", ctypes.c_double), ("vin", ctypes.c_double),
+                ("tin", ctypes.c_double), ("t_wall", ctypes.c_double), ("resimax", ctypes.c_double),
+                ("nswpp", ctypes.c_int), ("order", ctypes.c_int), ("iter_t_bug", ctypes.c_int),
+                ("thermal", ctypes.c_int), ("res_every", ctypes.c_int)]
+
+
+class Coeffs(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("time", "cfl", "cpb", "cd", "cl", "cd_p", "cd_v", "cl_p", "cl_v", "nu")] + \
+               [("sweeps", ctypes.c_int), ("resid", ctypes.c_double)]
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement with its Makefile (portable flags, no FMA contraction)."""
+    src = os.path.join(HERE, "fvm_oracle.c")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.POINTER(Params)]
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        P = ctypes.POINTER(ctypes.c_double)
+        L.orc_set_grid.argtypes = [ctypes.c_void_p, P, P]
+        L.orc_init.argtypes = [ctypes.c_void_p, P, P]
+        L.orc_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_last_coeffs.restype = ctypes.POINTER(Coeffs)
+        L.orc_last_coeffs.argtypes = [ctypes.c_void_p]
+        L.orc_array.restype = P
+        L.orc_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        L.orc_time.restype = ctypes.c_double
+        L.orc_time.argtypes = [ctypes.c_void_p]
+        L.orc_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        L.orc_sum_area.restype = ctypes.c_double
+        L.orc_sum_area.argtypes = [ctypes.c_void_p]
+        L.orc_iter_p.restype = ctypes.c_int
+        for f in ("orc_begin_step", "orc_contra_vel", "orc_explicit", "orc_iter_u", "orc_iter_v",
+                  "orc_remove_grad", "orc_iter_p", "orc_correct", "orc_iter_t", "orc_calccoef"):
+            getattr(L, f).argtypes = [ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Oracle:
+    """One case of the CPU restatement.  Arrays are numpy views shaped
+    (NJ+1, NI+1): a[j, i] is the reference's (I, J)."""
+
+    def __init__(self, ni, nj, re=100.0, pr=0.71, dt=0.005, vel_rot=0.0, order=GPU,
+                 resimax=1e-10, nswpp=100000, thermal=True, iter_t_bug=True, res_every=1,
+                 uin=1.0, vin=0.0, tin=0.0, t_wall=1.0):
+        self.ni, self.nj = ni, nj
+        p = Params(ni=ni, nj=nj, re=re, pr=pr, dt=dt, vel_rot=vel_rot, uin=uin, vin=vin, tin=tin,
+                   t_wall=t_wall, resimax=resimax, nswpp=nswpp, order=order,
+                   iter_t_bug=int(iter_t_bug), thermal=int(thermal), res_every=res_every)
+        self._p = p
+        self._h = lib().orc_create(ctypes.byref(p))
+        if not self._h:
+            raise ValueError("orc_create failed")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().orc_destroy(h)
+            self._h = None
+
+    def set_grid(self, xg, yg):
+        xg = np.ascontiguousarray(xg, dtype=np.float64).ravel()
+        yg = np.ascontiguousarray(yg, dtype=np.float64).ravel()
+        rc = lib().orc_set_grid(self._h, _dptr(xg), _dptr(yg))
+        if rc != 0:
+            raise ValueError(f"orc_set_grid failed ({rc})")
+
+    def init(self, du=None, dv=None):
+        a = None if du is None else np.ascontiguousarray(du, dtype=np.float64).ravel()
+        b = None if dv is None else np.ascontiguousarray(dv, dtype=np.float64).ravel()
+        lib().orc_init(self._h, None if a is None else _dptr(a), None if b is None else _dptr(b))
+
+    def step(self, n=1):
+        rc = lib().orc_step(self._h, n)
+        if rc != 0:
+            raise FloatingPointError(f"orc_step failed ({rc})")
+
+    def call(self, name):
+        return getattr(lib(), "orc_" + name)(self._h)
+
+    def array(self, name) -> np.ndarray:
+        p = lib().orc_array(self._h, name.encode())
+        if not p:
+            raise KeyError(name)
+        return np.ctypeslib.as_array(p, shape=(self.nj + 1, self.ni + 1))
+
+    def coeffs(self) -> dict:
+        c = lib().orc_last_coeffs(self._h).contents
+        return {n: getattr(c, n) for n, _ in Coeffs._fields_}
+
+    @property
+    def time(self):
+        return lib().orc_time(self._h)
+
+    def set_time(self, t, niter=0):
+        lib().orc_set_time(self._h, t, niter)
