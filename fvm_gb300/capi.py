@@ -1,0 +1,221 @@
+"""ctypes binding of the C-ABI in include/fvm.h.
+
+This is the Python face of the same entry points a Fortran driver binds through
+ISO_C_BINDING.  The CUDA library must be present: loading raises if it is not
+(there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FVM_OK, FVM_ERR_ARG, FVM_ERR_CUDA, FVM_ERR_NOCONV, FVM_ERR_TIMEOUT, FVM_ERR_NAN, FVM_ERR_NOMEM = range(7)
+FP64, MIXED = 0, 1
+FIELD_U, FIELD_V, FIELD_T = 0, 1, 2
+
+STATUS_NAMES = {0: "FVM_OK", 1: "FVM_ERR_ARG", 2: "FVM_ERR_CUDA", 3: "FVM_ERR_NOCONV",
+                4: "FVM_ERR_TIMEOUT", 5: "FVM_ERR_NAN", 6: "FVM_ERR_NOMEM"}
+
+# Every symbol include/fvm.h declares (checked by the CPU tests).
+EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", "fvm_set_grid",
+           "fvm_init", "fvm_upload_state", "fvm_download_state", "fvm_get_array", "fvm_set_array",
+           "fvm_set_time", "fvm_begin_step", "fvm_contra_vel", "fvm_nl", "fvm_dif", "fvm_p_source",
+           "fvm_iter_u", "fvm_iter_v", "fvm_remove_grad", "fvm_iter_p", "fvm_correct", "fvm_iter_t",
+           "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize"]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("ni", ctypes.c_int), ("nj", ctypes.c_int),
+                ("re", ctypes.c_double), ("pr", ctypes.c_double), ("dt", ctypes.c_double),
+                ("vel_rot", ctypes.c_double), ("uin", ctypes.c_double), ("vin", ctypes.c_double),
+                ("tin", ctypes.c_double), ("t_wall", ctypes.c_double), ("resimax", ctypes.c_double),
+                ("nswpp", ctypes.c_int), ("precision", ctypes.c_int), ("thermal", ctypes.c_int),
+                ("iter_t_bug", ctypes.c_int), ("res_every", ctypes.c_int),
+                ("refine_sweeps", ctypes.c_int), ("adi_refine", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class Coeffs(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("time", "cfl", "cpb", "cd", "cl", "cd_p", "cd_v", "cl_p", "cl_v", "nu")] + \
+               [("sweeps", ctypes.c_int), ("resid", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class FvmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libfvm_gb300.so (building it in-tree first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ImportError(f"CUDA library {path} is missing; run fvm_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    D = ctypes.POINTER(ctypes.c_double)
+    V = ctypes.c_void_p
+    L.fvm_default_params.argtypes = [ctypes.POINTER(Params)]
+    L.fvm_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(V)]
+    L.fvm_destroy.argtypes = [V]
+    L.fvm_last_error.argtypes = [V]
+    L.fvm_last_error.restype = ctypes.c_char_p
+    L.fvm_set_grid.argtypes = [V, D, D]
+    L.fvm_init.argtypes = [V, D, D]
+    L.fvm_upload_state.argtypes = [V] + [D] * 7
+    L.fvm_download_state.argtypes = [V] + [D] * 7
+    L.fvm_get_array.argtypes = [V, ctypes.c_char_p, D]
+    L.fvm_set_array.argtypes = [V, ctypes.c_char_p, D]
+    L.fvm_set_time.argtypes = [V, ctypes.c_double, ctypes.c_int]
+    for f in ("fvm_begin_step", "fvm_contra_vel", "fvm_p_source", "fvm_iter_u", "fvm_iter_v",
+              "fvm_remove_grad", "fvm_correct", "fvm_iter_t", "fvm_synchronize"):
+        getattr(L, f).argtypes = [V]
+    L.fvm_nl.argtypes = [V, ctypes.c_int]
+    L.fvm_dif.argtypes = [V, ctypes.c_int]
+    L.fvm_iter_p.argtypes = [V, D, ctypes.POINTER(ctypes.c_int)]
+    L.fvm_calccoef.argtypes = [V, ctypes.POINTER(Coeffs)]
+    L.fvm_step.argtypes = [V, ctypes.c_int, ctypes.POINTER(Coeffs)]
+    L.fvm_history.argtypes = [V, ctypes.POINTER(Coeffs), ctypes.c_int]
+    _lib = L
+    return L
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    load().fvm_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _arr(a, n):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    if a.size != n:
+        raise ValueError(f"array has {a.size} elements, expected {n}")
+    return a
+
+
+class Context:
+    """One solver context (one CUDA stream on one GPU).  Field arrays are numpy
+    arrays shaped (NJ+1, NI+1): a[j, i] is the reference's (I, J)."""
+
+    def __init__(self, params: Params):
+        self.L = load()
+        self.p = params
+        self.ni, self.nj = params.ni, params.nj
+        self.n = (self.ni + 1) * (self.nj + 1)
+        h = ctypes.c_void_p()
+        rc = self.L.fvm_create(ctypes.byref(params), ctypes.byref(h))
+        if rc != FVM_OK:
+            raise FvmError(rc, "fvm_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fvm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc, allow=()):
+        if rc != FVM_OK and rc not in allow:
+            raise FvmError(rc, self.L.fvm_last_error(self.h).decode())
+        return rc
+
+    def last_error(self) -> str:
+        return self.L.fvm_last_error(self.h).decode()
+
+    # set-up ------------------------------------------------------------------
+    def set_grid(self, xg, yg):
+        x, y = _arr(xg, self.n), _arr(yg, self.n)
+        self._ok(self.L.fvm_set_grid(self.h, _dp(x), _dp(y)))
+
+    def init(self, du=None, dv=None):
+        a, b = _arr(du, self.n), _arr(dv, self.n)
+        self._ok(self.L.fvm_init(self.h, _dp(a), _dp(b)))
+
+    # state -------------------------------------------------------------------
+    def upload(self, u=None, v=None, p=None, t=None, nlx=None, nly=None, adv=None):
+        arrs = [_arr(a, self.n) for a in (u, v, p, t, nlx, nly, adv)]
+        self._ok(self.L.fvm_upload_state(self.h, *[_dp(a) for a in arrs]))
+
+    def download(self, names=("U", "V", "P", "T")):
+        return {nm: self.get(nm) for nm in names}
+
+    def get(self, name) -> np.ndarray:
+        out = np.empty(self.n)
+        self._ok(self.L.fvm_get_array(self.h, name.encode(), _dp(out)))
+        return out.reshape(self.nj + 1, self.ni + 1)
+
+    def set(self, name, a):
+        a = _arr(a, self.n)
+        self._ok(self.L.fvm_set_array(self.h, name.encode(), _dp(a)))
+
+    def set_time(self, t, niter=0):
+        self._ok(self.L.fvm_set_time(self.h, t, niter))
+
+    # reference call points -----------------------------------------------------
+    def begin_step(self): self._ok(self.L.fvm_begin_step(self.h))
+    def contra_vel(self): self._ok(self.L.fvm_contra_vel(self.h))
+    def nl(self, field): self._ok(self.L.fvm_nl(self.h, field))
+    def dif(self, field): self._ok(self.L.fvm_dif(self.h, field))
+    def p_source(self): self._ok(self.L.fvm_p_source(self.h))
+    def iter_u(self): self._ok(self.L.fvm_iter_u(self.h))
+    def iter_v(self): self._ok(self.L.fvm_iter_v(self.h))
+    def remove_grad(self): self._ok(self.L.fvm_remove_grad(self.h))
+    def correct(self): self._ok(self.L.fvm_correct(self.h))
+    def iter_t(self): self._ok(self.L.fvm_iter_t(self.h))
+
+    def iter_p(self):
+        r = ctypes.c_double()
+        s = ctypes.c_int()
+        rc = self._ok(self.L.fvm_iter_p(self.h, ctypes.byref(r), ctypes.byref(s)), allow=(FVM_ERR_NOCONV,))
+        return r.value, s.value, rc
+
+    def calccoef(self) -> dict:
+        c = Coeffs()
+        self._ok(self.L.fvm_calccoef(self.h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def step(self, n=1) -> dict:
+        c = Coeffs()
+        self._ok(self.L.fvm_step(self.h, n, ctypes.byref(c)), allow=(FVM_ERR_NOCONV,))
+        return c.as_dict()
+
+    def history(self, n):
+        arr = (Coeffs * n)()
+        self._ok(self.L.fvm_history(self.h, arr, n))
+        return [a.as_dict() for a in arr]
+
+    def synchronize(self):
+        self._ok(self.L.fvm_synchronize(self.h))

@@ -1,0 +1,264 @@
+// fvm_internal.cuh -- device data layout, context and shared device helpers of the
+// GB300 cylinder time step.  All arrays live in one device slab; every field array
+// is the reference's Fortran (0:NI,0:NJ) array, element (i,j) at i + (NI+1)*j.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/fvm.h"
+
+namespace fvm {
+
+constexpr int WARP = 32;
+
+// One set of constant tridiagonal factors for a family of lines (one line per
+// radial row j, or per circumferential column i).  Factors are stored
+// lane-interleaved: element e = lane*M + k of line L sits at L*32*M + k*32 + lane,
+// so every warp-wide load of one k is coalesced.  Padding elements (e >= n) have
+// zero factors and never influence real elements.
+struct LineSys {
+    int lines = 0;     // number of lines
+    int n = 0;         // unknowns per line
+    int M = 0;         // elements per lane (ceil(n/32))
+    int cyclic = 0;    // 1: periodic line solved by Sherman-Morrison
+    double *invD = nullptr, *fa = nullptr, *fb = nullptr, *z = nullptr;  // FP64 factors
+    float *invDf = nullptr, *faf = nullptr, *fbf = nullptr, *zf = nullptr; // FP32 copies
+    double *cv = nullptr, *sinv = nullptr;   // cyclic: a_1/gamma and 1/(1+v.z) per line
+    float *cvf = nullptr, *sinvf = nullptr;
+};
+
+// Five-point coefficient set of one AF factor or of the Poisson operator, with the
+// boundary-condition folding already applied (constant for the run).
+struct Coef {
+    double *AP = nullptr, *AE = nullptr, *AW = nullptr, *AN = nullptr, *AS = nullptr;
+    float *ANf = nullptr, *ASf = nullptr, *AEf = nullptr, *AWf = nullptr;
+    double *awall = nullptr;   // raw AW(1,j) before folding (per j)
+    double *afar = nullptr;    // raw AE(NI-1,j) before folding (per j)
+};
+
+// Device control block of the Poisson iteration.
+struct PCtl {
+    int niter;          // sweeps done in the current ITER_P
+    int done;           // 1 once converged or capped
+    int capped;         // 1 if stopped at the cap above tolerance
+    int pad;
+    double resip;       // last scaled residual
+    unsigned int ticket;
+    unsigned int pad2;
+    double cflmax_bits_dummy;
+};
+
+// Everything a kernel needs, passed by value.
+struct Dev {
+    int NI, NJ, NI1, n;
+    double re, pe, dt, rdt, vel_rot, uin, vin, tin, t_wall, pi, resimax;
+    int nswpp, res_every, iter_t_bug, refine_sweeps;
+    // geometry
+    double *XG, *YG, *X, *Y, *XIX, *XIY, *ETX, *ETY, *DJAC, *Q11, *Q12, *Q22;
+    double *DE, *DW, *DN, *DS, *THETA, *AREA;
+    double *JQ12;          // DJAC*Q12
+    double *JXE, *JYE;     // (DJAC*XIX)*ETX and (DJAC*XIY)*ETY
+    double *RJDT;          // (2*RE)*DJAC/DT  and for Pe:
+    double *PJDT;          // (2*PE)*DJAC/DT
+    double *UFW, *VFW, *TFW;  // wall boundary values per j (constant)
+    double *FFU, *FFV, *FFT;  // far-field boundary values per j (per step)
+    // state
+    double *U, *V, *P, *T, *U_N, *V_N, *T_N;
+    double *NLX, *NLY, *ADV, *NLX_NM1, *NLY_NM1, *ADV_NM1, *DIFX, *DIFY, *DIFT, *S_U, *S_V;
+    double *UE, *UW, *VN, *VS, *DIVDT;
+    double *SU, *SUV, *SUT, *DD;   // per-field right-hand sides (U uses SU)
+    // mixed-precision scratch
+    float *RF, *DF;                // FP32 residual right-hand side and correction
+    double *W64;                   // FP64 scratch line values (defect correction)
+    // reductions
+    PCtl *pctl;
+    double *partial;               // per-block partial sums (2 per block)
+    double *coefrow;               // per-j CALCCOEF contributions (6 per j)
+    unsigned long long *cflbits;
+    double *scal;                  // small scalars: [0]=sum_area
+    // line systems and coefficients
+    Coef cP, cUX, cUY, cTX, cTY;
+    LineSys sP, sUX, sUY, sTX, sTY;
+};
+
+}  // namespace fvm
+
+struct fvm_ctx {
+    fvm_params p{};
+    int NI = 0, NJ = 0, NI1 = 0, n = 0;
+    cudaStream_t stream = nullptr;
+    fvm::Dev d{};
+    char *slab = nullptr;
+    size_t slab_bytes = 0;
+    std::string err;
+    bool grid_set = false, init_done = false;
+    double rtime = 0.0;
+    int niter_time = 0;
+    fvm_coeffs last{};
+    std::vector<fvm_coeffs> hist;
+    fvm::PCtl *h_pctl = nullptr;     // pinned mirror
+    // Poisson graph: a batch of sweeps replayed until converged
+    cudaGraphExec_t pgraph = nullptr;
+    int pgraph_batch = 0;
+    int pgraph_mode = -1;
+    int nblk_res = 0;
+};
+
+// ---------------------------------------------------------------------------------
+// Host helpers shared by the translation units
+// ---------------------------------------------------------------------------------
+#define FVM_CUDA(ctx, call)                                                                  \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+            return FVM_ERR_CUDA;                                                             \
+        }                                                                                    \
+    } while (0)
+
+#define FVM_LAUNCH_CHECK(ctx)                                                                \
+    do {                                                                                     \
+        cudaError_t e_ = cudaGetLastError();                                                 \
+        if (e_ != cudaSuccess) {                                                             \
+            (ctx)->err = std::string("kernel launch: ") + cudaGetErrorString(e_);            \
+            return FVM_ERR_CUDA;                                                             \
+        }                                                                                    \
+    } while (0)
+
+namespace fvm {
+int setup_allocate(fvm_ctx *c);
+int setup_grid(fvm_ctx *c);
+int setup_init(fvm_ctx *c, const double *du, const double *dv);
+int run_begin_step(fvm_ctx *c);
+int run_contra_vel(fvm_ctx *c);
+int run_nl(fvm_ctx *c, int field);
+int run_dif(fvm_ctx *c, int field);
+int run_p_source(fvm_ctx *c);
+int run_iter_u(fvm_ctx *c, int field);
+int run_remove_grad(fvm_ctx *c);
+int run_iter_p(fvm_ctx *c, double *resid, int *sweeps);
+int run_correct(fvm_ctx *c);
+int run_iter_t(fvm_ctx *c);
+int run_calccoef(fvm_ctx *c, fvm_coeffs *out);
+int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out);
+double *array_by_name(fvm_ctx *c, const char *name);
+}  // namespace fvm
+
+// ---------------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------------
+#define IDX(i, j) ((i) + d.NI1 * (j))
+
+namespace fvm {
+
+// Ghost cells derived from interior cell (i,j) after it takes value val: the wall
+// ghost (i=1), the far-field ghost (i=NI-1) of the Dirichlet-by-ghost condition
+// phi_ghost = -phi + 2 phi_boundary (bcu.f90:18,38), and the branch-cut copies
+// (bcu.f90:44-51), including the corner cells the reference fills by the copy.
+__device__ __forceinline__ void ghost_dirichlet(const Dev &d, double *phi, int i, int j, double val,
+                                                const double *wallF, const double *farF)
+{
+    const int NI = d.NI, NJ = d.NJ;
+    if (i == 1) {
+        double g = (-val) + 2.0 * wallF[j];
+        phi[IDX(0, j)] = g;
+        if (j == 1) phi[IDX(0, NJ)] = g;
+        if (j == NJ - 1) phi[IDX(0, 0)] = g;
+    }
+    if (i == NI - 1) {
+        double g = (-val) + 2.0 * farF[j];
+        phi[IDX(NI, j)] = g;
+        if (j == 1) phi[IDX(NI, NJ)] = g;
+        if (j == NJ - 1) phi[IDX(NI, 0)] = g;
+    }
+    if (j == 1) phi[IDX(i, NJ)] = val;
+    if (j == NJ - 1) phi[IDX(i, 0)] = val;
+}
+
+__device__ __forceinline__ int jwrap(const Dev &d, int j)
+{
+    return j == 0 ? d.NJ - 1 : (j == d.NJ ? 1 : j);
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_up(T v, int s) { return __shfl_up_sync(0xffffffffu, v, s); }
+template <typename T>
+__device__ __forceinline__ T shfl_down(T v, int s) { return __shfl_down_sync(0xffffffffu, v, s); }
+template <typename T>
+__device__ __forceinline__ T shfl_idx(T v, int s) { return __shfl_sync(0xffffffffu, v, s); }
+
+// Apply the precomputed LU factors of one line to the right-hand side held in
+// v[0..M-1] (lane owns elements lane*M .. lane*M+M-1), in place.
+//   forward:  y_e = invD_e r_e + fa_e y_{e-1}
+//   backward: x_e = y_e + fb_e x_{e+1}
+// Each first-order recurrence is split into per-lane chunks, combined across the
+// warp by a Kogge-Stone scan of affine maps, and fixed up.  f* point at the line's
+// factor block (lane-interleaved).
+template <typename T, int M>
+__device__ __forceinline__ void line_apply(T (&v)[M], const T *__restrict__ invD,
+                                           const T *__restrict__ fa, const T *__restrict__ fb, int lane)
+{
+    T gk[M];
+    T y = T(0), g = T(1);
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        T a = fa[k * WARP + lane];
+        y = a * y + invD[k * WARP + lane] * v[k];
+        v[k] = y;
+        g = g * a;
+        gk[k] = g;
+    }
+    T G = g, Y = y;
+#pragma unroll
+    for (int s = 1; s < WARP; s <<= 1) {
+        T Gp = shfl_up(G, s), Yp = shfl_up(Y, s);
+        if (lane >= s) { Y = Y + G * Yp; G = G * Gp; }
+    }
+    T yin = shfl_up(Y, 1);
+    if (lane == 0) yin = T(0);
+#pragma unroll
+    for (int k = 0; k < M; k++) v[k] = v[k] + gk[k] * yin;
+
+    T x = T(0), h = T(1);
+#pragma unroll
+    for (int k = M - 1; k >= 0; k--) {
+        T b = fb[k * WARP + lane];
+        x = v[k] + b * x;
+        v[k] = x;
+        h = h * b;
+        gk[k] = h;
+    }
+    T H = h, X = x;
+#pragma unroll
+    for (int s = 1; s < WARP; s <<= 1) {
+        T Hn = shfl_down(H, s), Xn = shfl_down(X, s);
+        if (lane + s < WARP) { X = X + H * Xn; H = H * Hn; }
+    }
+    T xin = shfl_down(X, 1);
+    if (lane == WARP - 1) xin = T(0);
+#pragma unroll
+    for (int k = 0; k < M; k++) v[k] = v[k] + gk[k] * xin;
+}
+
+// Sherman-Morrison completion of a cyclic line after line_apply on the modified
+// matrix: x = y - ((y_1 + cv*y_n) * sinv) z.
+template <typename T, int M>
+__device__ __forceinline__ void line_cyclic_fix(T (&v)[M], const T *__restrict__ z, T cv, T sinv, int n, int lane)
+{
+    T y1 = shfl_idx(v[0], 0);
+    const int last = n - 1, ll = last / M, lk = last % M;
+    T yl = T(0);
+#pragma unroll
+    for (int k = 0; k < M; k++)
+        if (k == lk) yl = v[k];
+    yl = shfl_idx(yl, ll);
+    T w = (y1 + cv * yl) * sinv;
+#pragma unroll
+    for (int k = 0; k < M; k++) v[k] = v[k] - w * z[k * WARP + lane];
+}
+
+}  // namespace fvm

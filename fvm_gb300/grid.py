@@ -99,7 +99,7 @@ def write_grid_file(path: str, g: OGrid) -> None:
     with open(path, "w") as f:
         for j in range(1, g.nj + 1):
             for i in range(1, g.ni + 1):
-                f.write(f"{g.xg[j, i]!r} {g.yg[j, i]!r}\n")
+                f.write(f"{float(g.xg[j, i])!r} {float(g.yg[j, i])!r}\n")
 
 
 def read_grid_file(path: str, ni: int, nj: int) -> OGrid:

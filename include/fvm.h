@@ -1,0 +1,127 @@
+/*
+ * fvm.h -- C-ABI of the GB300 time step of the fractional 4-step incompressible
+ * Navier-Stokes finite-volume solver on a curvilinear cylinder O-grid.
+ *
+ * Drop-in boundary.  The reference (Fortran 90, cylinder/cylinder_v3.0.3_AF_
+ * original 4step_face_nl/) drives one time step from PROGRAM MAIN
+ * (Main.f90:48-114) through argument-less subroutines sharing module globals
+ * (comdat_shared.f90).  This library owns those globals on the GPU: a context
+ * holds every field, metric and scratch array in device memory, and each entry
+ * point below replaces one call point of the reference's time loop.  All
+ * functions take plain pointers and sizes, are callable from Fortran through
+ * ISO_C_BINDING (BIND(C)), and return an int status (FVM_OK = 0) -- they never
+ * abort.  fvm_last_error() gives the message of the last failure.
+ *
+ * Array layout: every field array is the reference's Fortran array (0:NI,0:NJ)
+ * of DOUBLE PRECISION, element (I,J) at index I + (NI+1)*J (I radial, I=0 the
+ * wall ghost, I=NI the far-field ghost; J circumferential, J=0 and J=NJ the
+ * branch-cut ghosts).  Node coordinates XG, YG use the same (NI+1)*(NJ+1)
+ * storage with I = 1..NI, J = 1..NJ valid.
+ *
+ * Threading: one context = one CUDA stream on one device.  Distinct contexts
+ * may be used from distinct host threads; one context must not be used by two
+ * threads at once.  Host arrays are only read or written during the call that
+ * receives them; no pointer is retained.
+ */
+#ifndef FVM_GB300_H
+#define FVM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    FVM_OK = 0,
+    FVM_ERR_ARG = 1,      /* invalid argument or call order */
+    FVM_ERR_CUDA = 2,     /* CUDA runtime error (message in fvm_last_error) */
+    FVM_ERR_NOCONV = 3,   /* Poisson sweep cap reached above tolerance (fields are valid) */
+    FVM_ERR_TIMEOUT = 4,  /* a bounded device-side wait ran out */
+    FVM_ERR_NAN = 5,      /* non-finite value detected in the step's coefficients */
+    FVM_ERR_NOMEM = 6     /* device allocation failed */
+};
+
+enum { FVM_FP64 = 0, FVM_MIXED = 1 };       /* precision of the line sweeps */
+enum { FVM_FIELD_U = 0, FVM_FIELD_V = 1, FVM_FIELD_T = 2 };
+
+/* Run parameters.  The reference takes NI, NJ, NSWPP, RESIMAX, UIN, VIN, TIN,
+ * T_WALL as compile-time PARAMETERs (comdat_param.f90:6-39) and RE, PR,
+ * VEL_ROT, DTIME from standard input (Main.f90:23-36). */
+typedef struct fvm_params {
+    int ni, nj;            /* NI, NJ: node counts; cells 1..NI-1 x 1..NJ-1; NJ-1 must be even */
+    double re, pr, dt, vel_rot;
+    double uin, vin, tin, t_wall;
+    double resimax;        /* Poisson scaled-L1 residual tolerance (RESIMAX) */
+    int nswpp;             /* Poisson sweep cap (NSWPP) */
+    int precision;         /* FVM_FP64 or FVM_MIXED */
+    int thermal;           /* 1: advance the passive temperature (ITER_T) */
+    int iter_t_bug;        /* 1: keep the reference's V in ITER_T's second cross term */
+    int res_every;         /* FP64: evaluate the Poisson residual every k-th sweep (>=1) */
+    int refine_sweeps;     /* MIXED: FP32 zebra sweeps per FP64 residual/refinement */
+    int adi_refine;        /* MIXED: FP64 defect-correction passes per predictor line solve */
+    int device;            /* CUDA device ordinal */
+} fvm_params;
+
+/* Per-step diagnostics of CALCCOEF (calccoef.f90:9-120) plus Poisson statistics. */
+typedef struct fvm_coeffs {
+    double time, cfl, cpb, cd, cl, cd_p, cd_v, cl_p, cl_v, nu;
+    int sweeps;            /* Poisson sweeps of the last step */
+    double resid;          /* last scaled residual of the last step */
+} fvm_coeffs;
+
+/* Defaults: the reference's PARAMETER values (comdat_param.f90:11-19), FP64. */
+int fvm_default_params(fvm_params *p);
+
+/* Context life cycle.  Replaces the module COMDAT_SHARED (comdat_shared.f90:38-162). */
+int fvm_create(const fvm_params *p, struct fvm_ctx **ctx);
+int fvm_destroy(struct fvm_ctx *ctx);
+const char *fvm_last_error(const struct fvm_ctx *ctx);
+
+/* GRID + METRIC (grid.f90:28-114, metric.f90:18-168) from node coordinates. */
+int fvm_set_grid(struct fvm_ctx *ctx, const double *xg, const double *yg);
+/* INIT (init.f90:17-137): uniform flow; du/dv (may be NULL) are added to the
+ * interior of U and V before the boundary conditions. */
+int fvm_init(struct fvm_ctx *ctx, const double *du, const double *dv);
+
+/* Host <-> device copies of the time-step state (the RESTART.DAT contents,
+ * writedata.f90:77-90).  Any pointer may be NULL to skip that array. */
+int fvm_upload_state(struct fvm_ctx *ctx, const double *u, const double *v, const double *p,
+                     const double *t, const double *nlx, const double *nly, const double *adv);
+int fvm_download_state(struct fvm_ctx *ctx, double *u, double *v, double *p, double *t,
+                       double *nlx, double *nly, double *adv);
+/* Named access to any context array (names as in comdat_shared.f90, e.g.
+ * "U", "DJAC", "S_U", "UE"); out/in hold (NI+1)*(NJ+1) doubles. */
+int fvm_get_array(struct fvm_ctx *ctx, const char *name, double *out);
+int fvm_set_array(struct fvm_ctx *ctx, const char *name, const double *in);
+int fvm_set_time(struct fvm_ctx *ctx, double rtime, int niter_time);
+
+/* One call point each of the reference time loop (Main.f90:48-114). */
+int fvm_begin_step(struct fvm_ctx *ctx);   /* Main.f90:48-54: time advance, U_N=U, V_N=V, T_N=T */
+int fvm_contra_vel(struct fvm_ctx *ctx);   /* CONTRA_VEL, contra_vel.f90:9-21,125 */
+int fvm_nl(struct fvm_ctx *ctx, int field);   /* NL(U_N,NLX) etc., nl.f90:21-27 (shifts *_NM1 first) */
+int fvm_dif(struct fvm_ctx *ctx, int field);  /* DIF(U_N,DIFX) etc., dif.f90 + dif_diagonal.f90 */
+int fvm_p_source(struct fvm_ctx *ctx);     /* P_SOURCE, p_source.f90:9-27 */
+int fvm_iter_u(struct fvm_ctx *ctx);       /* ITER_U, iter_u.f90:13-119 (with BCU) */
+int fvm_iter_v(struct fvm_ctx *ctx);       /* ITER_V, iter_v.f90 (with BCV) */
+int fvm_remove_grad(struct fvm_ctx *ctx);  /* Main.f90:80-87: u^ = u* - dt S/J, BCU, BCV */
+/* Main.f90:91-93: CONTRA_VEL, ITER_P (iter_p.f90:12-51 with LISOLV and BCP), BCP.
+ * resid/sweeps may be NULL.  Returns FVM_ERR_NOCONV if the cap was reached. */
+int fvm_iter_p(struct fvm_ctx *ctx, double *resid, int *sweeps);
+int fvm_correct(struct fvm_ctx *ctx);      /* Main.f90:97-107: P_SOURCE, u += dt S/J, BCU, BCV */
+int fvm_iter_t(struct fvm_ctx *ctx);       /* Main.f90:110-111: ITER_T (iter_T.f90) and BCT */
+int fvm_calccoef(struct fvm_ctx *ctx, fvm_coeffs *out);  /* CALCCOEF, calccoef.f90:9-120 */
+
+/* nsteps complete time steps (Main.f90:48-114 without file output), state kept
+ * on the device.  out (may be NULL) receives the last step's coefficients.
+ * Returns FVM_ERR_NOCONV if any step hit the sweep cap (the run continues, as in
+ * the reference). */
+int fvm_step(struct fvm_ctx *ctx, int nsteps, fvm_coeffs *out);
+/* Per-step coefficient history of the last fvm_step call: n entries copied. */
+int fvm_history(struct fvm_ctx *ctx, fvm_coeffs *out, int n);
+
+/* Block until all work queued on the context's stream has finished. */
+int fvm_synchronize(struct fvm_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
