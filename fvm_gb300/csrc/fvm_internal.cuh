@@ -49,18 +49,25 @@ struct PCtl {
     double resip;       // last scaled residual
     unsigned int ticket;
     unsigned int pad2;
-    double cflmax_bits_dummy;
+    double pad3;
 };
 
 // Everything a kernel needs, passed by value.
 struct Dev {
     int NI, NJ, NI1, n;
     double re, pe, dt, rdt, vel_rot, uin, vin, tin, t_wall, pi, resimax;
-    int nswpp, res_every, iter_t_bug, refine_sweeps;
+    int nswpp;          // sweep cap, rounded up to a multiple of the residual interval
+    int res_every;      // FP64: residual interval (even, >= 2)
+    int iter_t_bug;
+    int refine_sweeps;  // MIXED: FP32 sweeps per FP64 refinement
+    int adi_refine;     // MIXED: defect-correction passes of a predictor line
     // geometry
     double *XG, *YG, *X, *Y, *XIX, *XIY, *ETX, *ETY, *DJAC, *Q11, *Q12, *Q22;
     double *DE, *DW, *DN, *DS, *THETA, *AREA;
     double *JQ12;          // DJAC*Q12
+    // Poisson cross term DD = CNE P(i+1,j+1) + CSE P(i+1,j-1) + CNW P(i-1,j+1) + CSW P(i-1,j-1),
+    // the four diagonal weights of dif_diagonal.f90:13-23 gathered per cell (interior)
+    double *CNE, *CSE, *CNW, *CSW;
     double *JXE, *JYE;     // (DJAC*XIX)*ETX and (DJAC*XIY)*ETY
     double *RJDT;          // (2*RE)*DJAC/DT  and for Pe:
     double *PJDT;          // (2*PE)*DJAC/DT
@@ -68,6 +75,7 @@ struct Dev {
     double *FFU, *FFV, *FFT;  // far-field boundary values per j (per step)
     // state
     double *U, *V, *P, *T, *U_N, *V_N, *T_N;
+    double *P2;            // second pressure buffer of the double-buffered FP64 zebra sweep
     double *NLX, *NLY, *ADV, *NLX_NM1, *NLY_NM1, *ADV_NM1, *DIFX, *DIFY, *DIFT, *S_U, *S_V;
     double *UE, *UW, *VN, *VS, *DIVDT;
     double *SU, *SUV, *SUT, *DD;   // per-field right-hand sides (U uses SU)
@@ -104,8 +112,7 @@ struct fvm_ctx {
     // Poisson graph: a batch of sweeps replayed until converged
     cudaGraphExec_t pgraph = nullptr;
     int pgraph_batch = 0;
-    int pgraph_mode = -1;
-    int nblk_res = 0;
+    int nblk_res = 0;      // blocks of the residual kernels
 };
 
 // ---------------------------------------------------------------------------------
@@ -146,6 +153,12 @@ int run_iter_t(fvm_ctx *c);
 int run_calccoef(fvm_ctx *c, fvm_coeffs *out);
 int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out);
 double *array_by_name(fvm_ctx *c, const char *name);
+// mixed precision (fvm_mixed.cu)
+int mixed_poisson_capture(fvm_ctx *c, int outer);
+int mixed_predictor_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi,
+                           int colour, int refresh, const double *wallF, const double *farF);
+int mixed_predictor_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi,
+                          int colour, int ghosts, const double *wallF, const double *farF);
 }  // namespace fvm
 
 // ---------------------------------------------------------------------------------

@@ -71,11 +71,11 @@ void carve(Bump &b, fvm_ctx *c, int nblk)
     const int nj1 = c->NJ + 1;
     double **geo[] = {&d.XG, &d.YG, &d.X, &d.Y, &d.XIX, &d.XIY, &d.ETX, &d.ETY, &d.DJAC, &d.Q11,
                       &d.Q12, &d.Q22, &d.DE, &d.DW, &d.DN, &d.DS, &d.THETA, &d.AREA, &d.JQ12,
-                      &d.JXE, &d.JYE, &d.RJDT, &d.PJDT};
+                      &d.JXE, &d.JYE, &d.RJDT, &d.PJDT, &d.CNE, &d.CSE, &d.CNW, &d.CSW};
     for (auto p : geo) *p = b.take<double>(n);
     double **perj[] = {&d.UFW, &d.VFW, &d.TFW, &d.FFU, &d.FFV, &d.FFT};
     for (auto p : perj) *p = b.take<double>(nj1);
-    double **st[] = {&d.U, &d.V, &d.P, &d.T, &d.U_N, &d.V_N, &d.T_N, &d.NLX, &d.NLY, &d.ADV,
+    double **st[] = {&d.U, &d.V, &d.P, &d.P2, &d.T, &d.U_N, &d.V_N, &d.T_N, &d.NLX, &d.NLY, &d.ADV,
                      &d.NLX_NM1, &d.NLY_NM1, &d.ADV_NM1, &d.DIFX, &d.DIFY, &d.DIFT, &d.S_U,
                      &d.S_V, &d.UE, &d.UW, &d.VN, &d.VS, &d.DIVDT, &d.SU, &d.SUV, &d.SUT,
                      &d.DD, &d.W64};
@@ -120,12 +120,19 @@ int setup_allocate(fvm_ctx *c)
     d.t_wall = c->p.t_wall;
     d.pi = 4.0 * std::atan(1.0);
     d.resimax = c->p.resimax;
-    d.nswpp = c->p.nswpp;
-    d.res_every = c->p.res_every < 1 ? 1 : c->p.res_every;
+    // The FP64 sweep alternates two pressure buffers, so its residual interval is
+    // even; the MIXED path checks after every refine_sweeps sweeps.  The sweep cap
+    // is rounded up to a multiple of the interval in use.
+    int re_ = c->p.res_every < 2 ? 2 : c->p.res_every + (c->p.res_every & 1);
+    int rs_ = c->p.refine_sweeps < 1 ? 1 : c->p.refine_sweeps;
+    d.res_every = re_;
+    d.refine_sweeps = rs_;
+    int k_ = c->p.precision == FVM_MIXED ? rs_ : re_;
+    d.nswpp = ((c->p.nswpp + k_ - 1) / k_) * k_;
     d.iter_t_bug = c->p.iter_t_bug;
-    d.refine_sweeps = c->p.refine_sweeps < 1 ? 1 : c->p.refine_sweeps;
+    d.adi_refine = c->p.adi_refine < 1 ? 1 : c->p.adi_refine;
     const int interior = (c->NI - 1) * (c->NJ - 1);
-    c->nblk_res = (interior + 255) / 256;
+    c->nblk_res = (interior + 1023) / 1024;   // residual kernels: 256 threads x 4 cells
     Bump probe{nullptr};
     carve(probe, c, c->nblk_res);
     c->slab_bytes = probe.off + 256;
@@ -239,6 +246,18 @@ __global__ void k_dcoef(Dev d)
     d.RJDT[c] = (2.0 * d.re) * J[c] / d.dt;
     d.PJDT[c] = (2.0 * d.pe) * J[c] / d.dt;
     if (i < 1 || i > d.NI - 1 || j < 1 || j > d.NJ - 1) return;
+    {   // diagonal weights of the cross term 0.25*(Ke(fne-fse) - Kw(fnw-fsw) + Kn(fne-fnw) - Ks(fse-fsw))
+        const double *K = d.JQ12;
+        double ke = __dmul_rn(J[IDX(i + 1, j)], d.Q12[IDX(i + 1, j)]);
+        double kw = __dmul_rn(J[IDX(i - 1, j)], d.Q12[IDX(i - 1, j)]);
+        double kn = __dmul_rn(J[IDX(i, j + 1)], d.Q12[IDX(i, j + 1)]);
+        double ks = __dmul_rn(J[IDX(i, j - 1)], d.Q12[IDX(i, j - 1)]);
+        (void)K;
+        d.CNE[c] = 0.25 * (ke + kn);
+        d.CSE[c] = -(0.25 * (ke + ks));
+        d.CNW[c] = -(0.25 * (kw + kn));
+        d.CSW[c] = 0.25 * (kw + ks);
+    }
     const double *Q1 = d.Q11, *Q2 = d.Q22;
     int e = IDX(i + 1, j), w = IDX(i - 1, j), nn = IDX(i, j + 1), s = IDX(i, j - 1);
     d.DE[c] = 0.5 * __dadd_rn(__dmul_rn(J[c], Q1[c]), __dmul_rn(J[e], Q1[e]));

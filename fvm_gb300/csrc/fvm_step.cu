@@ -12,98 +12,9 @@
 #include <cstring>
 
 #include "fvm_internal.cuh"
+#include "fvm_ops.cuh"
 
 namespace fvm {
-
-// ---------------------------------------------------------------------------------
-// Cell operators (shared by the per-routine and the fused kernels)
-// ---------------------------------------------------------------------------------
-__device__ __forceinline__ double nl_at(const Dev &d, const double *in, int i, int j)
-{   // NL (nl.f90:21-27)
-    int c = IDX(i, j);
-    double t1 = (d.UE[c] * 0.5) * (in[c] + in[IDX(i + 1, j)]);
-    double t2 = (d.UW[c] * 0.5) * (in[c] + in[IDX(i - 1, j)]);
-    double t3 = (d.VN[c] * 0.5) * (in[c] + in[IDX(i, j + 1)]);
-    double t4 = (d.VS[c] * 0.5) * (in[c] + in[IDX(i, j - 1)]);
-    return ((t1 - t2) + t3) - t4;
-}
-
-// Cross-derivative term 0.25*sum(+-K*(diagonal differences)) with K = coefficient
-// array evaluated at the four face neighbours (dif_diagonal.f90:13-23 with K=J*Q12;
-// iter_u.f90:31-41 with K=J*xix*etx and K=J*xiy*ety).
-__device__ __forceinline__ double cross_at(const Dev &d, const double *K, const double *f, int i, int j)
-{
-    double fne = f[IDX(i + 1, j + 1)], fse = f[IDX(i + 1, j - 1)];
-    double fnw = f[IDX(i - 1, j + 1)], fsw = f[IDX(i - 1, j - 1)];
-    double t1 = K[IDX(i + 1, j)] * (fne - fse);
-    double t2 = K[IDX(i - 1, j)] * (fnw - fsw);
-    double t3 = K[IDX(i, j + 1)] * (fne - fnw);
-    double t4 = K[IDX(i, j - 1)] * (fse - fsw);
-    return 0.25 * (((t1 - t2) + t3) - t4);
-}
-
-__device__ __forceinline__ double dif_at(const Dev &d, const double *in, int i, int j)
-{   // DIF (dif.f90:13-23)
-    int c = IDX(i, j);
-    double dd = cross_at(d, d.JQ12, in, i, j);
-    double p = in[c];
-    double a = d.DE[c] * (in[IDX(i + 1, j)] - p);
-    double b = d.DW[c] * (in[IDX(i - 1, j)] - p);
-    double e = d.DN[c] * (in[IDX(i, j + 1)] - p);
-    double f = d.DS[c] * (in[IDX(i, j - 1)] - p);
-    return (((a + b) + e) + f) + dd;
-}
-
-__device__ __forceinline__ void psource_at(const Dev &d, int i, int j, double &su, double &sv)
-{   // P_SOURCE (p_source.f90:9-27); P ghost values are read as stored
-    const double *J = d.DJAC, *P = d.P;
-    int e = IDX(i + 1, j), w = IDX(i - 1, j), nn = IDX(i, j + 1), s = IDX(i, j - 1);
-    double a = ((((J[e] * d.XIX[e]) * P[e] - (J[w] * d.XIX[w]) * P[w]) + (J[nn] * d.ETX[nn]) * P[nn]) - (J[s] * d.ETX[s]) * P[s]);
-    double b = ((((J[e] * d.XIY[e]) * P[e] - (J[w] * d.XIY[w]) * P[w]) + (J[nn] * d.ETY[nn]) * P[nn]) - (J[s] * d.ETY[s]) * P[s]);
-    su = -(0.5 * a);
-    sv = -(0.5 * b);
-}
-
-__device__ __forceinline__ double u1_at(const Dev &d, int c) { return d.XIX[c] * d.U[c] + d.XIY[c] * d.V[c]; }
-__device__ __forceinline__ double u2_at(const Dev &d, int c) { return d.ETX[c] * d.U[c] + d.ETY[c] * d.V[c]; }
-
-// Predictor right-hand side of the first AF factor (iter_u.f90:31-46) with the
-// wall/far-field folding of BCU (bcu.f90:15, 35).
-__device__ __forceinline__ double af_su1_at(const Dev &d, int kind, const double *phi, const double *phin,
-                                            const double *nl, const double *nlm1, const double *dif,
-                                            const double *src, int i, int j)
-{
-    int c = IDX(i, j);
-    const bool tk = (kind == FVM_FIELD_T);
-    const double rek = tk ? d.pe : d.re;
-    const double *JDT = tk ? d.PJDT : d.RJDT;
-    double s = (JDT[c] * phin[c] - (3.0 * rek) * nl[c]) + rek * nlm1[c];
-    s = s + dif[c];
-    if (!tk) s = s + (2.0 * rek) * src[c];
-    s = s + cross_at(d, d.JXE, phi, i, j);
-    const Coef &cf = tk ? d.cTX : d.cUX;
-    if (i == 1) {
-        double w = (kind == FVM_FIELD_U) ? d.UFW[j] : (kind == FVM_FIELD_V ? d.VFW[j] : d.TFW[j]);
-        s = s + (2.0 * cf.awall[j]) * w;
-    }
-    if (i == d.NI - 1) {
-        double f = (kind == FVM_FIELD_U) ? d.FFU[j] : (kind == FVM_FIELD_V ? d.FFV[j] : d.FFT[j]);
-        s = s + (2.0 * cf.afar[j]) * f;
-    }
-    return s;
-}
-
-struct FieldRefs {
-    double *phi, *phin, *nl, *nlm1, *dif, *src, *su;
-    const double *wallF, *farF;
-};
-
-__device__ __forceinline__ FieldRefs field_refs(const Dev &d, int kind)
-{
-    if (kind == FVM_FIELD_U) return {d.U, d.U_N, d.NLX, d.NLX_NM1, d.DIFX, d.S_U, d.SU, d.UFW, d.FFU};
-    if (kind == FVM_FIELD_V) return {d.V, d.V_N, d.NLY, d.NLY_NM1, d.DIFY, d.S_V, d.SUV, d.VFW, d.FFV};
-    return {d.T, d.T_N, d.ADV, d.ADV_NM1, d.DIFT, nullptr, d.SUT, d.TFW, d.FFT};
-}
 
 // ---------------------------------------------------------------------------------
 // Elementwise / stencil kernels.  Interior cells are mapped to a 2-D grid with i
@@ -143,8 +54,7 @@ __global__ void k_farfield_step(Dev d)
 }
 
 // CONTRA_VEL (contra_vel.f90:9-21,125); with_poisson additionally forms the
-// Poisson source (1/dt)*div and the first sweep's SU = div/dt - DD(P)
-// (iter_p.f90:24-30) and resets the iteration control.
+// Poisson source (1/dt)*div (iter_p.f90:27-29) and resets the iteration control.
 __global__ void k_contra_vel(Dev d, int with_poisson)
 {
     INTERIOR_IJ
@@ -160,9 +70,7 @@ __global__ void k_contra_vel(Dev d, int with_poisson)
     d.VN[c] = vn;
     d.VS[c] = vs;
     if (with_poisson) {
-        double dv = d.rdt * (((ue - uw) + vn) - vs);
-        d.DIVDT[c] = dv;
-        d.SU[c] = dv - cross_at(d, d.JQ12, d.P, i, j);
+        d.DIVDT[c] = d.rdt * (((ue - uw) + vn) - vs);
         if (i == 1 && j == 1) {
             d.pctl->niter = 0;
             d.pctl->done = 0;
@@ -326,38 +234,6 @@ __global__ void k_bcp_ghosts(Dev d)
 // ---------------------------------------------------------------------------------
 // Line sweeps (warp per line)
 // ---------------------------------------------------------------------------------
-enum { BCK_DIRICHLET = 0, BCK_POISSON = 1 };
-
-// Ghost values of radial row j taken from its current interior (the BC call that
-// precedes the sweep in the reference: BCU before iter_u.f90:50, BCP before
-// iter_p.f90:34).  Writes phi(0,j), phi(NI,j) and, for j = 1 / NJ-1, the
-// branch-cut row with its corners.
-template <int BCK>
-__device__ void refresh_row_ghosts(const Dev &d, double *phi, int j, const double *wallF, const double *farF, int lane)
-{
-    const int NI = d.NI, NJ = d.NJ;
-    double g0, gn;
-    if (BCK == BCK_POISSON) {
-        g0 = phi[IDX(1, j)];
-        gn = (3.0 * phi[IDX(NI - 1, j)] - 3.0 * phi[IDX(NI - 2, j)]) + phi[IDX(NI - 3, j)];
-    } else {
-        g0 = (-phi[IDX(1, j)]) + 2.0 * wallF[j];
-        gn = (-phi[IDX(NI - 1, j)]) + 2.0 * farF[j];
-    }
-    int rowdst = (j == 1) ? NJ : ((j == NJ - 1) ? 0 : -1);
-    if (rowdst >= 0) {
-        for (int i = 1 + lane; i <= NI - 1; i += WARP) phi[IDX(i, rowdst)] = phi[IDX(i, j)];
-    }
-    if (lane == 0) {
-        phi[IDX(0, j)] = g0;
-        phi[IDX(NI, j)] = gn;
-        if (rowdst >= 0) {
-            phi[IDX(0, rowdst)] = g0;
-            phi[IDX(NI, rowdst)] = gn;
-        }
-    }
-}
-
 // Zebra radial-line sweep: lines j of one colour (colour 0: odd j) solve
 //   -AW x(i-1) + AP x(i) - AE x(i+1) = AN phi(i,j+1) + AS phi(i,j-1) + SU
 // with the neighbour rows read through periodic wrap (lisolv.f90:72-84,
@@ -376,8 +252,8 @@ __global__ void __launch_bounds__(128) k_radial(Dev d, LineSys s, Coef cf, const
     const int jn = jwrap(d, j + 1), js = jwrap(d, j - 1);
     const int n = s.n;
     if (refresh) {
-        refresh_row_ghosts<BCK>(d, phi, j, wallF, farF, lane);
-        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK>(d, phi, j + 1, wallF, farF, lane);
+        refresh_row_ghosts<BCK>(d, phi, phi, j, wallF, farF, lane);
+        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK>(d, phi, phi, j + 1, wallF, farF, lane);
         __syncwarp();
     }
     double v[M];
@@ -438,80 +314,80 @@ __global__ void __launch_bounds__(128) k_theta(Dev d, LineSys s, Coef cf, const 
 }
 
 // ---------------------------------------------------------------------------------
-// Poisson residual (iter_p.f90:37-51) fused with the next sweep's lagged cross term
-// (iter_p.f90:24-30).  Deterministic two-level reduction; the last block decides
-// convergence and publishes the iteration count.
+// FP64 pressure Poisson (iter_p.f90:22-51, lisolv.f90:18-33, bcp.f90:8-42).
+// One outer iteration = lagged cross term DD from the iteration's input, BCP ghost
+// refresh from that input, a zebra line sweep, and (every res_every-th iteration)
+// the scaled-L1 residual.  The sweep reads its input P^(n-1) from Pin and writes
+// P^n to Pout (two alternating buffers): colour 0 (odd rows) reads its neighbour
+// rows from Pin, colour 1 (even rows) from Pout, exactly the in-place zebra order,
+// while DD of both colours still sees P^(n-1) as the reference's lagged term does.
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ void block_sum2(double &a, double &b, double *sh)
+template <int M>
+__global__ void __launch_bounds__(128) k_pois64(Dev d, const double *Pin, double *Pout, int colour)
 {
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
+    if (d.pctl->done) return;
+    const int lane = threadIdx.x & (WARP - 1);
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) / WARP;
+    if (w >= (d.NJ - 1) / 2) return;
+    const int j = 2 * w + 1 + colour;
+    const int jn = jwrap(d, j + 1), js = jwrap(d, j - 1);
+    const LineSys &s = d.sP;
+    const Coef &cf = d.cP;
+    const int n = s.n;
+    if (colour == 0) {   // BCP of this iteration: ghosts of P^(n-1), stored with P^n
+        refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j, nullptr, nullptr, lane);
+        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j + 1, nullptr, nullptr, lane);
     }
-    const int wid = threadIdx.x / WARP, lane = threadIdx.x & 31, nw = blockDim.x / WARP;
-    __syncthreads();
-    if (lane == 0) { sh[2 * wid] = a; sh[2 * wid + 1] = b; }
-    __syncthreads();
-    if (wid == 0) {
-        a = lane < nw ? sh[2 * lane] : 0.0;
-        b = lane < nw ? sh[2 * lane + 1] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_down_sync(0xffffffffu, a, o);
-            b += __shfl_down_sync(0xffffffffu, b, o);
+    const double *Pnb = colour ? Pout : Pin;
+    double v[M];
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        int e = lane * M + k;
+        v[k] = 0.0;
+        if (e < n) {
+            int i = e + 1, c = IDX(i, j);
+            double su = d.DIVDT[c] - dd_p(d, Pin, i, j);
+            v[k] = (cf.AN[c] * Pnb[IDX(i, jn)] + cf.AS[c] * Pnb[IDX(i, js)]) + su;
         }
+    }
+    const size_t base = size_t(j - 1) * WARP * M;
+    line_apply<double, M>(v, s.invD + base, s.fa + base, s.fb + base, lane);
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        int e = lane * M + k;
+        if (e < n) Pout[IDX(e + 1, j)] = v[k];
     }
 }
 
-__global__ void __launch_bounds__(256) k_pres(Dev d)
+// Residual after an even number of iterations: P^n in P, P^(n-1) in P2.  SU of the
+// last sweep is rebuilt from P^(n-1) (with its stored ghosts).  The last block
+// publishes the count and decides convergence (iter_p.f90:50-51).
+__global__ void __launch_bounds__(256) k_pres64(Dev d)
 {
     __shared__ double sh[64];
     __shared__ bool last;
     if (d.pctl->done) return;
-    const int it = d.pctl->niter + 1;
-    const bool check = (it % d.res_every == 0) || (it >= d.nswpp);
-    const int NI = d.NI, ni1 = NI - 1;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int it = d.pctl->niter + d.res_every;
+    const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
     double ra = 0.0, pa = 0.0;
-    if (e < ni1 * (d.NJ - 1)) {
-        const int i = e % ni1 + 1, j = e / ni1 + 1;
-        const int c = IDX(i, j);
-        const double *P = d.P;
-        if (check) {
-            const Coef &cf = d.cP;
-            double p = P[c];
-            double r = ((((cf.AE[c] * P[IDX(i + 1, j)] + cf.AW[c] * P[IDX(i - 1, j)]) + cf.AN[c] * P[IDX(i, jwrap(d, j + 1))])
-                         + cf.AS[c] * P[IDX(i, jwrap(d, j - 1))]) + d.SU[c]) - cf.AP[c] * p;
-            ra = fabs(r);
-            pa = fabs(cf.AP[c] * p);
+    for (int q = 0; q < 4; q++) {
+        int e = blockIdx.x * 1024 + q * 256 + threadIdx.x;
+        if (e < total) {
+            int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
+            double su = d.DIVDT[c] - dd_p(d, d.P2, i, j);
+            double r = pres_at(d, d.P, su, i, j);
+            ra += fabs(r);
+            pa += fabs(d.cP.AP[c] * d.P[c]);
         }
-        d.SU[c] = d.DIVDT[c] - cross_at(d, d.JQ12, P, i, j);
     }
-    block_sum2(ra, pa, sh);
+    if (!grid_sum2(d, ra, pa, sh, last)) return;
     if (threadIdx.x == 0) {
-        d.partial[2 * blockIdx.x] = ra;
-        d.partial[2 * blockIdx.x + 1] = pa;
-        __threadfence();
-        unsigned t = atomicInc(&d.pctl->ticket, gridDim.x - 1);
-        last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
-        a += ((volatile double *)d.partial)[2 * k];
-        b += ((volatile double *)d.partial)[2 * k + 1];
-    }
-    block_sum2(a, b, sh);
-    if (threadIdx.x == 0) {
+        double resip = ra / pa;
         d.pctl->niter = it;
-        if (check) {
-            double resip = a / b;
-            d.pctl->resip = resip;
-            if (!(resip > d.resimax && it < d.nswpp)) {
-                d.pctl->done = 1;
-                d.pctl->capped = (resip > d.resimax) ? 1 : 0;
-            }
+        d.pctl->resip = resip;
+        if (!(resip > d.resimax && it < d.nswpp)) {
+            d.pctl->done = 1;
+            d.pctl->capped = (resip > d.resimax) ? 1 : 0;
         }
     }
 }
@@ -663,15 +539,20 @@ int predictor_sweeps(fvm_ctx *c, int field)
     double *su = field == FVM_FIELD_U ? d.SU : (field == FVM_FIELD_V ? d.SUV : d.SUT);
     const double *wf = field == FVM_FIELD_U ? d.UFW : (field == FVM_FIELD_V ? d.VFW : d.TFW);
     const double *farF = field == FVM_FIELD_U ? d.FFU : (field == FVM_FIELD_V ? d.FFV : d.FFT);
+    const bool mixed = c->p.precision == FVM_MIXED;
     // sweep 1 (radial lines), ghosts refreshed from the pre-sweep field (BCU)
-    RC(launch_radial<BCK_DIRICHLET>(c, sx, cx, su, phi, 0, 1, wf, farF, 0));
-    RC(launch_radial<BCK_DIRICHLET>(c, sx, cx, su, phi, 1, 0, wf, farF, 0));
+    for (int colour = 0; colour < 2; colour++) {
+        if (mixed) RC(mixed_predictor_radial(c, sx, cx, su, phi, colour, colour == 0, wf, farF));
+        else RC(launch_radial<BCK_DIRICHLET>(c, sx, cx, su, phi, colour, colour == 0, wf, farF, 0));
+    }
     // second factor right-hand side from the first-sweep field
     const double *xf = (tk && c->p.iter_t_bug) ? d.V : phi;
     k_af_su2<<<interior_grid(c), 128, 0, c->stream>>>(d, field, xf);
     FVM_LAUNCH_CHECK(c);
-    RC(launch_theta(c, sy, cy, su, phi, 0, tk ? 1 : 0, wf, farF));
-    RC(launch_theta(c, sy, cy, su, phi, 1, tk ? 1 : 0, wf, farF));
+    for (int colour = 0; colour < 2; colour++) {
+        if (mixed) RC(mixed_predictor_theta(c, sy, cy, su, phi, colour, tk ? 1 : 0, wf, farF));
+        else RC(launch_theta(c, sy, cy, su, phi, colour, tk ? 1 : 0, wf, farF));
+    }
     return FVM_OK;
 }
 
@@ -730,22 +611,58 @@ int run_remove_grad(fvm_ctx *c)
     return FVM_OK;
 }
 
-static int poisson_graph(fvm_ctx *c, int batch)
+int launch_pois64(fvm_ctx *c, const double *Pin, double *Pout, int colour)
 {
-    if (c->pgraph && c->pgraph_batch == batch) return FVM_OK;
-    if (c->pgraph) {
-        cudaGraphExecDestroy(c->pgraph);
-        c->pgraph = nullptr;
+    const int half = (c->NJ - 1) / 2;
+    const int blocks = (half * WARP + 127) / 128;
+    const Dev &d = c->d;
+    switch (d.sP.M) {
+#define CASE(MM)                                                                                   \
+    case MM:                                                                                       \
+        k_pois64<MM><<<blocks, 128, 0, c->stream>>>(d, Pin, Pout, colour);                         \
+        break;
+        CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
+        CASE(9) CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16)
+#undef CASE
+    default:
+        c->err = "line length above 512 cells is not supported";
+        return FVM_ERR_ARG;
     }
+    FVM_LAUNCH_CHECK(c);
+    return FVM_OK;
+}
+
+// Capture `groups` residual intervals of the FP64 iteration into one graph:
+// res_every sweeps alternating P -> P2 -> P, then the residual.
+static int poisson64_capture(fvm_ctx *c, int groups)
+{
     Dev &d = c->d;
+    int rc = FVM_OK;
+    for (int g = 0; g < groups && rc == FVM_OK; g++) {
+        for (int it = 0; it < d.res_every && rc == FVM_OK; it++) {
+            const double *in = (it & 1) ? d.P2 : d.P;
+            double *out = (it & 1) ? d.P : d.P2;
+            rc = launch_pois64(c, in, out, 0);
+            if (rc == FVM_OK) rc = launch_pois64(c, in, out, 1);
+        }
+        if (rc == FVM_OK) {
+            k_pres64<<<c->nblk_res, 256, 0, c->stream>>>(d);
+            FVM_LAUNCH_CHECK(c);
+        }
+    }
+    return rc;
+}
+
+static int poisson_graph(fvm_ctx *c)
+{
+    if (c->pgraph) return FVM_OK;
+    Dev &d = c->d;
+    const bool mixed = c->p.precision == FVM_MIXED;
+    const int per = mixed ? d.refine_sweeps : d.res_every;
+    int groups = (32 + per - 1) / per;   // about 32 sweeps per replay
     cudaGraph_t g = nullptr;
     FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = FVM_OK;
-    for (int b = 0; b < batch && rc == FVM_OK; b++) {
-        rc = launch_radial<BCK_POISSON>(c, d.sP, d.cP, d.SU, d.P, 0, 1, nullptr, nullptr, 1);
-        if (rc == FVM_OK) rc = launch_radial<BCK_POISSON>(c, d.sP, d.cP, d.SU, d.P, 1, 0, nullptr, nullptr, 1);
-        if (rc == FVM_OK) k_pres<<<c->nblk_res, 256, 0, c->stream>>>(d);
-    }
+    int rc = mixed ? mixed_poisson_capture(c, groups) : poisson64_capture(c, groups);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc) {
         if (g) cudaGraphDestroy(g);
@@ -761,7 +678,7 @@ static int poisson_graph(fvm_ctx *c, int batch)
         c->err = std::string("Poisson graph instantiate: ") + cudaGetErrorString(e);
         return FVM_ERR_CUDA;
     }
-    c->pgraph_batch = batch;
+    c->pgraph_batch = groups * per;
     return FVM_OK;
 }
 
@@ -770,12 +687,11 @@ int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
     Dev &d = c->d;
     k_contra_vel<<<interior_grid(c), 128, 0, c->stream>>>(d, 1);
     FVM_LAUNCH_CHECK(c);
-    const int batch = 16;
-    RC(poisson_graph(c, batch));
+    RC(poisson_graph(c));
     int status = FVM_OK;
     // The device stops itself at the cap; the host bound only guards against a
     // control block that never reports completion.
-    const long max_launches = (long)c->p.nswpp / batch + 2;
+    const long max_launches = (long)d.nswpp / c->pgraph_batch + 2;
     for (long launch = 0;; launch++) {
         if (launch >= max_launches) {
             c->err = "Poisson iteration did not report completion within the sweep cap";

@@ -31,7 +31,7 @@ def make_case(n_theta=32, n_r=24, re=100.0, pr=0.71, dt=0.005, skew=0.0, amp=1e-
                 thermal=thermal, vel_rot=vel_rot)
 
 
-def make_oracle(case, order=oracle.GPU, res_every=1):
+def make_oracle(case, order=oracle.GPU, res_every=2):
     g = case["g"]
     o = oracle.Oracle(g.ni, g.nj, re=case["re"], pr=case["pr"], dt=case["dt"], vel_rot=case["vel_rot"],
                       order=order, resimax=case["resimax"], nswpp=case["nswpp"],
@@ -41,7 +41,7 @@ def make_oracle(case, order=oracle.GPU, res_every=1):
     return o
 
 
-def make_gpu(case, precision=capi.FP64, res_every=1, refine_sweeps=4, adi_refine=2):
+def make_gpu(case, precision=capi.FP64, res_every=2, refine_sweeps=4, adi_refine=2):
     g = case["g"]
     p = capi.default_params(ni=g.ni, nj=g.nj, re=case["re"], pr=case["pr"], dt=case["dt"],
                             vel_rot=case["vel_rot"], resimax=case["resimax"], nswpp=case["nswpp"],
