@@ -1,0 +1,385 @@
+#!/usr/bin/env python3
+"""Throughput of the cylinder time step on GB300 (Mcell-steps/s).
+
+Workload (one GPU): the 2-D Re=200 cylinder with passive temperature (Pr=0.71,
+wall T=1, inflow T=0) on the 512 (theta) x 384 (r) O-grid, wall radius 0.5 to
+50, first radial spacing 0.005 with the geometric ratio solved for the outer
+radius, dt=0.002, uniform start with a seeded +-1e-3 perturbation.  The Poisson
+iteration runs to the scaled-L1 tolerance 1e-10 under the reference's sweep cap
+NSWPP, set to 2000 so that every step does the same, reported, amount of line
+Gauss-Seidel work.  A step is one complete time step (Main.f90:48-114).
+
+value: the mixed-precision path (FP32 zebra sweeps in FP64 refinement); the FP64
+path is timed in the same run.  e2e: the same metric through the C-ABI with the
+state uploaded from and downloaded to pinned host memory every step.
+
+--impl reference times the CPU restatement of the reference (serial, the
+reference's execution model) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="cylinder2d-re200-thermal-512x384", n_theta=512, n_r=384, re=200.0, pr=0.71, dt=0.002,
+                resimax=1e-10, nswpp=2000, thermal=1, amp=1e-3, seed=0, dr1=0.005, r_out=50.0)
+METRIC = "Mcell-steps/s mixed vs FP64 GPU at <=1e-6 rel field error; adjoint/forward time"
+
+
+def cells(w):
+    return w["n_theta"] * w["n_r"]
+
+
+def case_inputs(w):
+    from fvm_gb300.grid import o_grid, perturbation
+    g = o_grid(w["n_theta"], w["n_r"], dr1=w["dr1"], r_out=w["r_out"])
+    du, dv = perturbation(g.ni, g.nj, w["amp"], w["seed"])
+    return g, du, dv
+
+
+# ---------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------------
+def make_ctx(w, precision, device, g, du, dv):
+    from fvm_gb300 import capi
+    p = capi.default_params(ni=g.ni, nj=g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], resimax=w["resimax"],
+                            nswpp=w["nswpp"], thermal=w["thermal"], precision=precision,
+                            res_every=2, refine_sweeps=8, adi_refine=2, device=device)
+    ctx = capi.Context(p)
+    ctx.set_grid(g.xg, g.yg)
+    ctx.init(du, dv)
+    return ctx
+
+
+def timed_steps(ctx, steps, flush, torch, ext):
+    """Time `steps` steps one at a time with CUDA events on the context's stream,
+    writing a buffer larger than L2 between steps (outside the events)."""
+    total = 0.0
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(ext)
+        ctx.step(1)
+        b.record(ext)
+        b.synchronize()
+        total += a.elapsed_time(b)
+    return total
+
+
+def cpu_baseline(w, g, du, dv, steps=2):
+    """Serial CPU restatement (reference order) on a bounded sample: the first
+    `steps` steps of the same workload."""
+    import oracle
+    o = oracle.Oracle(g.ni, g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], order=oracle.FAITHFUL,
+                      resimax=w["resimax"], nswpp=w["nswpp"], thermal=bool(w["thermal"]))
+    o.set_grid(g.xg, g.yg)
+    o.init(du, dv)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    sw = o.coeffs()["sweeps"]
+    return {"value": cells(w) * steps / dt / 1e6, "unit": "Mcell-steps/s", "cores": 1, "kind": "port",
+            "sample": f"first {steps} time steps of the same workload ({sw} Poisson sweeps in the last), "
+                      f"serial restatement in the reference's lexicographic order, {dt:.1f} s"}
+
+
+def roofline_sweep(w, timing, peaks, mixed):
+    """Algorithmic bytes of the Poisson sweep kernels over the measured in-graph
+    spans.  FP32 sweep (per launch, one colour): per active cell RF, ANf, ASf,
+    invDf, faf, fbf read and DF written (28 B) plus the other colour's DF read
+    once (4 B): 32 B x active cells; the span's last launch also updates P
+    (read+write 16 B per cell) and reads the odd rows' DF (4 B per odd cell).
+    FP64 sweep: per active cell DIVDT, 4 cross weights, AN, AS, 3 factors (80 B)
+    read and P written (8 B), plus the other colour's P read (8 B, 16 B for the
+    colour that also reads the lagged input): 100 B x active cells on average."""
+    n_active = cells(w) // 2
+    launches = timing["sweep_span_launches"]
+    ms = timing["sweep_span_ms"]
+    if launches <= 0 or ms <= 0:
+        return None
+    if mixed:
+        per_span_launch = 32.0 * n_active
+        k = 8
+        span_bytes = (2 * k * per_span_launch + 16.0 * cells(w) + 4.0 * n_active) * (launches / (2 * k))
+        unit_bytes = span_bytes
+    else:
+        unit_bytes = 100.0 * n_active * launches
+    avg_ms = ms / launches
+    achieved = unit_bytes / (ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs") if peaks else None
+    peak_src = "measured" if peak else "fallback"
+    if not peak:
+        peak = 6800.0
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "k_pois32" if mixed else "k_pois64",
+            "avg_launch_us": avg_ms * 1e3, "bytes_per_launch": unit_bytes / launches,
+            "peak_source": peak_src}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from fvm_gb300 import capi, dist
+
+    rank, world = dist.init("nccl")
+    local = dist.rank_world()[2]
+    torch.cuda.set_device(local)
+    w = dict(WORKLOAD)
+    g, du, dv = case_inputs(w)
+    capi.load()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MiB > L2
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+
+    res = {}
+    for name, prec in (("fp64", capi.FP64), ("mixed", capi.MIXED)):
+        ctx = make_ctx(w, prec, local, g, du, dv)
+        ext = torch.cuda.ExternalStream(ctx.stream_handle())
+        ctx.step(args.warmup)
+        ctx.timing_reset()
+        dist.barrier()
+        clk = ClockSampler(local) if name == "mixed" else None
+        if clk:
+            clk.start()
+        ms = timed_steps(ctx, args.steps, flush, torch, ext)
+        clocks = clk.stop() if clk else None
+        dist.barrier()
+        ms_max = dist.max_over_ranks(ms, device="cuda")
+        tm = ctx.timing()
+        hist = ctx.history(1)
+        fields = {nm: ctx.get(nm).copy() for nm in ("U", "V", "P", "T")}
+        res[name] = dict(ms=ms_max, timing=tm, clocks=clocks, sweeps=hist[0]["sweeps"], fields=fields,
+                         cd=hist[0]["cd"], resid=hist[0]["resid"])
+        ctx.close()
+
+    # e2e through the C-ABI with host buffers (mixed path)
+    ctx = make_ctx(w, capi.MIXED, local, g, du, dv)
+    ext = torch.cuda.ExternalStream(ctx.stream_handle())
+    ctx.step(args.warmup)
+    n = (g.ni + 1) * (g.nj + 1)
+    host = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(7)]
+    ptrs = [h.data_ptr() for h in host]
+    ctx.download_ptrs(ptrs)
+    e2e_ms = 0.0
+    dist.barrier()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(ext)
+        ctx.upload_ptrs(ptrs)
+        ctx.step(1)
+        ctx.download_ptrs(ptrs)
+        b.record(ext)
+        b.synchronize()
+        e2e_ms += a.elapsed_time(b)
+    dist.barrier()
+    e2e_ms = dist.max_over_ranks(e2e_ms, device="cuda")
+    ctx.close()
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    field_err = {nm: rel(res["mixed"]["fields"][nm], res["fp64"]["fields"][nm]) for nm in ("U", "V", "P", "T")}
+    units = world * cells(w) * args.steps
+    value = units / (res["mixed"]["ms"] * 1e-3) / 1e6
+    fp64_value = units / (res["fp64"]["ms"] * 1e-3) / 1e6
+    e2e_value = units / (e2e_ms * 1e-3) / 1e6
+    roof = roofline_sweep(w, res["mixed"]["timing"], peaks, True)
+    roof64 = roofline_sweep(w, res["fp64"]["timing"], peaks, False)
+    traffic_file = os.path.join(ROOT, "profiles", "k_pois32_cylinder2d_512x384.json")
+    if roof and os.path.exists(traffic_file):
+        try:
+            roof["traffic"] = json.load(open(traffic_file)).get("dram_bytes_per_launch")
+        except Exception:
+            roof["traffic"] = None
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["mixed"]["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": w["name"], "grid": f"{w['n_theta']} theta x {w['n_r']} r cells",
+                   "cells": cells(w), "re": w["re"], "pr": w["pr"], "dt": w["dt"],
+                   "poisson": f"zebra line GS to scaled-L1 {w['resimax']:g}, cap NSWPP={w['nswpp']}",
+                   "sweeps_per_step": res["mixed"]["sweeps"], "precision": "mixed: FP32 zebra sweeps in FP64 "
+                   "refinement every 8 sweeps, FP32 predictor lines with 2 FP64 defect-correction passes; "
+                   "state, metrics and residuals FP64",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "256 MiB buffer written between timed steps (outside the events)"},
+        "fp64": {"value": fp64_value, "ms_per_step": res["fp64"]["ms"] / args.steps,
+                 "sweeps_per_step": res["fp64"]["sweeps"], "roofline": roof64},
+        "mixed_vs_fp64": {"speedup": value / fp64_value, "field_rel_l2": field_err,
+                          "cd_rel": abs(res["mixed"]["cd"] - res["fp64"]["cd"]) / abs(res["fp64"]["cd"])},
+        "roofline": roof,
+        "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 7 * n * 8,
+                "d2h_bytes_per_step": 7 * n * 8 + 96},
+        "gpu_launches": int(res["mixed"]["timing"]["kernel_launches"]),
+        "clocks": res["mixed"]["clocks"],
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(w, g, du, dv)
+    elif rank == 0:
+        out["cpu_baseline"] = None
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    dist.finalize()
+
+
+# ---------------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------------
+def run_reference(args):
+    from fvm_gb300 import dist
+    rank, world, _ = dist.rank_world()
+    if rank != 0:
+        return
+    import oracle
+    w = dict(WORKLOAD)
+    g, du, dv = case_inputs(w)
+    o = oracle.Oracle(g.ni, g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], order=oracle.FAITHFUL,
+                      resimax=w["resimax"], nswpp=w["nswpp"], thermal=bool(w["thermal"]))
+    o.set_grid(g.xg, g.yg)
+    o.init(du, dv)
+    # Each step is timed by sub-step so that a long run can sample fewer Poisson
+    # sweeps per step and scale the Poisson part to the full sweep count.
+    budget_s = 200.0
+    est_step = None
+    sample_sweeps = w["nswpp"]
+
+    def one_step(nswpp_sample):
+        t0 = time.perf_counter()
+        for f in ("begin_step", "contra_vel", "explicit", "iter_u", "iter_v", "remove_grad"):
+            o.call(f)
+        t1 = time.perf_counter()
+        sw = o.call("iter_p")
+        t2 = time.perf_counter()
+        o.call("correct")
+        if w["thermal"]:
+            o.call("iter_t")
+        o.call("calccoef")
+        t3 = time.perf_counter()
+        return (t1 - t0) + (t3 - t2), t2 - t1, sw
+
+    # the oracle reads its parameters at creation: rebuild with the sample cap when needed
+    def rebuild(cap):
+        nonlocal o
+        o = oracle.Oracle(g.ni, g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], order=oracle.FAITHFUL,
+                          resimax=w["resimax"], nswpp=cap, thermal=bool(w["thermal"]))
+        o.set_grid(g.xg, g.yg)
+        o.init(du, dv)
+
+    t_fix, t_p, sw = one_step(w["nswpp"])   # probe step (counts as warm-up)
+    est_step = t_fix + t_p
+    total_steps = args.warmup + args.steps
+    if total_steps * est_step > budget_s:
+        sample_sweeps = max(20, int(w["nswpp"] * budget_s / (total_steps * est_step)))
+        rebuild(sample_sweeps)
+    for _ in range(max(0, args.warmup - 1)):
+        one_step(sample_sweeps)
+    tot = 0.0
+    for _ in range(args.steps):
+        tf, tp, swn = one_step(sample_sweeps)
+        tot += tf + tp * (w["nswpp"] / max(swn, 1))
+    value = cells(w) * args.steps / tot / 1e6
+    sample = (f"CPU restatement, reference (lexicographic) order, serial; {args.steps} steps of the workload"
+              + ("" if sample_sweeps == w["nswpp"] else
+                 f", Poisson sampled at {sample_sweeps} of {w['nswpp']} sweeps per step and scaled"))
+    out = {"metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": {"workload": w["name"], "cells": cells(w),
+                      "poisson": f"line GS to scaled-L1 {w['resimax']:g}, cap NSWPP={w['nswpp']}"},
+           "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": 1, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -25,7 +25,8 @@ EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", 
            "fvm_init", "fvm_upload_state", "fvm_download_state", "fvm_get_array", "fvm_set_array",
            "fvm_set_time", "fvm_begin_step", "fvm_contra_vel", "fvm_nl", "fvm_dif", "fvm_p_source",
            "fvm_iter_u", "fvm_iter_v", "fvm_remove_grad", "fvm_iter_p", "fvm_correct", "fvm_iter_t",
-           "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize"]
+           "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize", "fvm_get_stream",
+           "fvm_timing_reset", "fvm_get_timing"]
 
 
 class Params(ctypes.Structure):
@@ -42,6 +43,15 @@ class Coeffs(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in
                 ("time", "cfl", "cpb", "cd", "cl", "cd_p", "cd_v", "cl_p", "cl_v", "nu")] + \
                [("sweeps", ctypes.c_int), ("resid", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Timing(ctypes.Structure):
+    _fields_ = [("sweep_span_ms", ctypes.c_double), ("sweep_span_launches", ctypes.c_longlong),
+                ("kernel_launches", ctypes.c_longlong), ("sweeps", ctypes.c_longlong),
+                ("steps", ctypes.c_longlong)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -94,6 +104,9 @@ def load(build_if_missing: bool = True):
     L.fvm_calccoef.argtypes = [V, ctypes.POINTER(Coeffs)]
     L.fvm_step.argtypes = [V, ctypes.c_int, ctypes.POINTER(Coeffs)]
     L.fvm_history.argtypes = [V, ctypes.POINTER(Coeffs), ctypes.c_int]
+    L.fvm_get_stream.argtypes = [V, ctypes.POINTER(ctypes.c_void_p)]
+    L.fvm_timing_reset.argtypes = [V]
+    L.fvm_get_timing.argtypes = [V, ctypes.POINTER(Timing)]
     _lib = L
     return L
 
@@ -219,3 +232,28 @@ class Context:
 
     def synchronize(self):
         self._ok(self.L.fvm_synchronize(self.h))
+
+    # instrumentation -----------------------------------------------------------
+    def stream_handle(self) -> int:
+        s = ctypes.c_void_p()
+        self._ok(self.L.fvm_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def timing_reset(self):
+        self._ok(self.L.fvm_timing_reset(self.h))
+
+    def timing(self) -> dict:
+        t = Timing()
+        self._ok(self.L.fvm_get_timing(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def upload_ptrs(self, ptrs):
+        """fvm_upload_state from raw host addresses (e.g. pinned buffers)."""
+        P = ctypes.POINTER(ctypes.c_double)
+        args = [ctypes.cast(p, P) if p else None for p in ptrs]
+        self._ok(self.L.fvm_upload_state(self.h, *args))
+
+    def download_ptrs(self, ptrs):
+        P = ctypes.POINTER(ctypes.c_double)
+        args = [ctypes.cast(p, P) if p else None for p in ptrs]
+        self._ok(self.L.fvm_download_state(self.h, *args))

@@ -83,6 +83,8 @@ int fvm_create(const fvm_params *p, fvm_ctx **out)
     cudaError_t e = cudaSetDevice(p->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_pctl, sizeof(fvm::PCtl));
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_a);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_b);
     if (e != cudaSuccess) {
         delete c;
         return FVM_ERR_CUDA;
@@ -103,6 +105,8 @@ int fvm_destroy(fvm_ctx *c)
     if (c->pgraph) cudaGraphExecDestroy(c->pgraph);
     if (c->slab) cudaFree(c->slab);
     if (c->h_pctl) cudaFreeHost(c->h_pctl);
+    if (c->ev_a) cudaEventDestroy(c->ev_a);
+    if (c->ev_b) cudaEventDestroy(c->ev_b);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FVM_OK;
@@ -240,6 +244,27 @@ int fvm_synchronize(fvm_ctx *c)
 {
     if (!c) return FVM_ERR_ARG;
     FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FVM_OK;
+}
+
+int fvm_get_stream(fvm_ctx *c, void **stream)
+{
+    if (!c || !stream) return FVM_ERR_ARG;
+    *stream = (void *)c->stream;
+    return FVM_OK;
+}
+
+int fvm_timing_reset(fvm_ctx *c)
+{
+    if (!c) return FVM_ERR_ARG;
+    c->tm = fvm_timing{};
+    return FVM_OK;
+}
+
+int fvm_get_timing(fvm_ctx *c, fvm_timing *out)
+{
+    if (!c || !out) return FVM_ERR_ARG;
+    *out = c->tm;
     return FVM_OK;
 }
 

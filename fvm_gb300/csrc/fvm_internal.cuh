@@ -113,7 +113,20 @@ struct fvm_ctx {
     cudaGraphExec_t pgraph = nullptr;
     int pgraph_batch = 0;
     int nblk_res = 0;      // blocks of the residual kernels
+    // instrumentation
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;   // span around the first sweep group of a replay
+    int pgraph_kernels = 0;                       // kernel nodes in the Poisson graph
+    int span_launches = 0;                        // sweep kernels inside the span
+    bool capturing = false;
+    fvm_timing tm{};
 };
+
+// Count one kernel launch of the context (into the graph being captured, if any).
+#define KCOUNT(c)                                             \
+    do {                                                      \
+        if ((c)->capturing) (c)->pgraph_kernels++;            \
+        else (c)->tm.kernel_launches++;                       \
+    } while (0)
 
 // ---------------------------------------------------------------------------------
 // Host helpers shared by the translation units

@@ -140,14 +140,22 @@ int mixed_poisson_capture(fvm_ctx *c, int outer)
     const int blocks = (half * WARP + 127) / 128;
     for (int o = 0; o < outer; o++) {
         k_mres<<<c->nblk_res, 256, 0, c->stream>>>(d);
+        KCOUNT(c);
         FVM_LAUNCH_CHECK(c);
+        if (o == 0) FVM_CUDA(c, cudaEventRecordWithFlags(c->ev_a, c->stream, cudaEventRecordExternal));
         for (int s = 0; s < d.refine_sweeps; s++) {
             const int apply = (s == d.refine_sweeps - 1);
             int rc = dispatch_m(c, d.sP.M, [&](auto m) {
                 k_pois32<decltype(m)::value><<<blocks, 128, 0, c->stream>>>(d, 0, 0);
                 k_pois32<decltype(m)::value><<<blocks, 128, 0, c->stream>>>(d, 1, apply);
+                KCOUNT(c);
+                KCOUNT(c);
             });
             if (rc) return rc;
+        }
+        if (o == 0) {
+            FVM_CUDA(c, cudaEventRecordWithFlags(c->ev_b, c->stream, cudaEventRecordExternal));
+            c->span_launches = 2 * d.refine_sweeps;
         }
     }
     return FVM_OK;
@@ -275,6 +283,7 @@ int mixed_predictor_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const d
     const Dev &d = c->d;
     return dispatch_m(c, s.M, [&](auto m) {
         k_rad_dc<decltype(m)::value><<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, refresh, wallF, farF);
+        KCOUNT(c);
     });
 }
 
@@ -286,6 +295,7 @@ int mixed_predictor_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const do
     const Dev &d = c->d;
     return dispatch_m(c, s.M, [&](auto m) {
         k_theta_dc<decltype(m)::value><<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, ghosts, wallF, farF);
+        KCOUNT(c);
     });
 }
 

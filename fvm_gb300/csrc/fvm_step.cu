@@ -486,6 +486,7 @@ int launch_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU
 #define CASE(MM)                                                                                   \
     case MM:                                                                                       \
         k_radial<MM, BCK><<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, refresh, wallF, farF, early_exit); \
+        KCOUNT(c);                                                                                 \
         break;
         CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
         CASE(9) CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16)
@@ -508,6 +509,7 @@ int launch_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU,
 #define CASE(MM)                                                                                   \
     case MM:                                                                                       \
         k_theta<MM><<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, ghosts, wallF, farF); \
+        KCOUNT(c);                                                                                 \
         break;
         CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
         CASE(9) CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16)
@@ -548,6 +550,7 @@ int predictor_sweeps(fvm_ctx *c, int field)
     // second factor right-hand side from the first-sweep field
     const double *xf = (tk && c->p.iter_t_bug) ? d.V : phi;
     k_af_su2<<<interior_grid(c), 128, 0, c->stream>>>(d, field, xf);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     for (int colour = 0; colour < 2; colour++) {
         if (mixed) RC(mixed_predictor_theta(c, sy, cy, su, phi, colour, tk ? 1 : 0, wf, farF));
@@ -564,7 +567,9 @@ int run_begin_step(fvm_ctx *c)
     c->rtime = c->rtime + c->p.dt;
     c->niter_time += 1;
     k_begin<<<(c->n + 255) / 256, 256, 0, c->stream>>>(d);
+    KCOUNT(c);
     k_farfield_step<<<(c->NJ + 127) / 128, 128, 0, c->stream>>>(d);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -572,6 +577,7 @@ int run_begin_step(fvm_ctx *c)
 int run_contra_vel(fvm_ctx *c)
 {
     k_contra_vel<<<interior_grid(c), 128, 0, c->stream>>>(c->d, 0);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -579,6 +585,7 @@ int run_contra_vel(fvm_ctx *c)
 int run_nl(fvm_ctx *c, int field)
 {
     k_nl<<<interior_grid(c), 128, 0, c->stream>>>(c->d, field);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -586,6 +593,7 @@ int run_nl(fvm_ctx *c, int field)
 int run_dif(fvm_ctx *c, int field)
 {
     k_dif<<<interior_grid(c), 128, 0, c->stream>>>(c->d, field);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -593,6 +601,7 @@ int run_dif(fvm_ctx *c, int field)
 int run_p_source(fvm_ctx *c)
 {
     k_psource<<<interior_grid(c), 128, 0, c->stream>>>(c->d);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -600,6 +609,7 @@ int run_p_source(fvm_ctx *c)
 int run_iter_u(fvm_ctx *c, int field)
 {
     k_af_su1<<<interior_grid(c), 128, 0, c->stream>>>(c->d, field);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return predictor_sweeps(c, field);
 }
@@ -607,6 +617,7 @@ int run_iter_u(fvm_ctx *c, int field)
 int run_remove_grad(fvm_ctx *c)
 {
     k_grad<<<interior_grid(c), 128, 0, c->stream>>>(c->d, -1.0, 0);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -620,6 +631,7 @@ int launch_pois64(fvm_ctx *c, const double *Pin, double *Pout, int colour)
 #define CASE(MM)                                                                                   \
     case MM:                                                                                       \
         k_pois64<MM><<<blocks, 128, 0, c->stream>>>(d, Pin, Pout, colour);                         \
+        KCOUNT(c);                                                                                 \
         break;
         CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
         CASE(9) CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16)
@@ -639,14 +651,20 @@ static int poisson64_capture(fvm_ctx *c, int groups)
     Dev &d = c->d;
     int rc = FVM_OK;
     for (int g = 0; g < groups && rc == FVM_OK; g++) {
+        if (g == 0) FVM_CUDA(c, cudaEventRecordWithFlags(c->ev_a, c->stream, cudaEventRecordExternal));
         for (int it = 0; it < d.res_every && rc == FVM_OK; it++) {
             const double *in = (it & 1) ? d.P2 : d.P;
             double *out = (it & 1) ? d.P : d.P2;
             rc = launch_pois64(c, in, out, 0);
             if (rc == FVM_OK) rc = launch_pois64(c, in, out, 1);
         }
+        if (g == 0) {
+            FVM_CUDA(c, cudaEventRecordWithFlags(c->ev_b, c->stream, cudaEventRecordExternal));
+            c->span_launches = 2 * d.res_every;
+        }
         if (rc == FVM_OK) {
             k_pres64<<<c->nblk_res, 256, 0, c->stream>>>(d);
+            KCOUNT(c);
             FVM_LAUNCH_CHECK(c);
         }
     }
@@ -662,7 +680,10 @@ static int poisson_graph(fvm_ctx *c)
     int groups = (32 + per - 1) / per;   // about 32 sweeps per replay
     cudaGraph_t g = nullptr;
     FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    c->pgraph_kernels = 0;
     int rc = mixed ? mixed_poisson_capture(c, groups) : poisson64_capture(c, groups);
+    c->capturing = false;
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc) {
         if (g) cudaGraphDestroy(g);
@@ -686,22 +707,38 @@ int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
 {
     Dev &d = c->d;
     k_contra_vel<<<interior_grid(c), 128, 0, c->stream>>>(d, 1);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     RC(poisson_graph(c));
     int status = FVM_OK;
     // The device stops itself at the cap; the host bound only guards against a
     // control block that never reports completion.
     const long max_launches = (long)d.nswpp / c->pgraph_batch + 2;
+    const int per = c->p.precision == FVM_MIXED ? d.refine_sweeps : d.res_every;
+    int n0 = 0;
     for (long launch = 0;; launch++) {
         if (launch >= max_launches) {
             c->err = "Poisson iteration did not report completion within the sweep cap";
             return FVM_ERR_TIMEOUT;
         }
         FVM_CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
+        c->tm.kernel_launches += c->pgraph_kernels;
         FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
         FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+        // the span holds real sweeps only if the replay advanced past its first group
+        if (c->h_pctl->niter >= n0 + per) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, c->ev_a, c->ev_b) == cudaSuccess) {
+                c->tm.sweep_span_ms += ms;
+                c->tm.sweep_span_launches += c->span_launches;
+            } else {
+                (void)cudaGetLastError();   // a missing sample is not an error of the step
+            }
+        }
+        n0 = c->h_pctl->niter;
         if (c->h_pctl->done) break;
     }
+    c->tm.sweeps += c->h_pctl->niter;
     if (c->h_pctl->capped) status = FVM_ERR_NOCONV;
     if (!std::isfinite(c->h_pctl->resip)) {
         c->err = "non-finite Poisson residual";
@@ -710,6 +747,7 @@ int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
     if (resid) *resid = c->h_pctl->resip;
     if (sweeps) *sweeps = c->h_pctl->niter;
     k_bcp_ghosts<<<(c->NI + c->NJ + 127) / 128, 128, 0, c->stream>>>(d);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return status;
 }
@@ -717,6 +755,7 @@ int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
 int run_correct(fvm_ctx *c)
 {
     k_grad<<<interior_grid(c), 128, 0, c->stream>>>(c->d, +1.0, 1);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -724,6 +763,7 @@ int run_correct(fvm_ctx *c)
 int run_iter_t(fvm_ctx *c)
 {
     k_af_su1<<<interior_grid(c), 128, 0, c->stream>>>(c->d, FVM_FIELD_T);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return predictor_sweeps(c, FVM_FIELD_T);
 }
@@ -732,10 +772,13 @@ int run_calccoef(fvm_ctx *c, fvm_coeffs *out)
 {
     Dev &d = c->d;
     k_calc_rows<<<(c->NJ + 127) / 128, 128, 0, c->stream>>>(d);
+    KCOUNT(c);
     k_cfl<<<interior_grid(c), 128, 0, c->stream>>>(d);
+    KCOUNT(c);
     fvm_coeffs *dout = reinterpret_cast<fvm_coeffs *>(d.scal + 4);
     static_assert(sizeof(fvm_coeffs) <= 12 * sizeof(double), "coeff scratch");
     k_calc_final<<<1, 1, 0, c->stream>>>(d, c->rtime, dout);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     FVM_CUDA(c, cudaMemcpyAsync(&c->last, dout, sizeof(fvm_coeffs), cudaMemcpyDeviceToHost, c->stream));
     FVM_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -755,7 +798,9 @@ int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out)
     for (int s = 0; s < nsteps; s++) {
         RC(run_begin_step(c));
         k_contra_vel<<<interior_grid(c), 128, 0, c->stream>>>(d, 0);
+        KCOUNT(c);
         k_explicit<<<interior_grid(c), 128, 0, c->stream>>>(d, c->p.thermal);
+        KCOUNT(c);
         FVM_LAUNCH_CHECK(c);
         RC(predictor_sweeps(c, FVM_FIELD_U));
         RC(predictor_sweeps(c, FVM_FIELD_V));
@@ -768,6 +813,7 @@ int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out)
         fvm_coeffs co;
         RC(run_calccoef(c, &co));
         c->hist.push_back(co);
+        c->tm.steps++;
         if (out) *out = co;
     }
     return status;

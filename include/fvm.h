@@ -121,6 +121,23 @@ int fvm_history(struct fvm_ctx *ctx, fvm_coeffs *out, int n);
 /* Block until all work queued on the context's stream has finished. */
 int fvm_synchronize(struct fvm_ctx *ctx);
 
+/* Instrumentation (no reference counterpart; used by benchmarks).  The CUDA
+ * stream of the context (a cudaStream_t), and counters accumulated since the last
+ * reset: CUDA-event time of spans that contain only Poisson sweep kernels inside
+ * the replayed Poisson graph (one span per replay, around the first group of
+ * sweeps), the number of sweep launches in those spans, every kernel the context
+ * launched, Poisson sweeps and time steps. */
+typedef struct fvm_timing {
+    double sweep_span_ms;
+    long long sweep_span_launches;
+    long long kernel_launches;
+    long long sweeps;
+    long long steps;
+} fvm_timing;
+int fvm_get_stream(struct fvm_ctx *ctx, void **stream);
+int fvm_timing_reset(struct fvm_ctx *ctx);
+int fvm_get_timing(struct fvm_ctx *ctx, fvm_timing *out);
+
 #ifdef __cplusplus
 }
 #endif
