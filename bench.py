@@ -6,8 +6,9 @@ wall T=1, inflow T=0) on the 512 (theta) x 384 (r) O-grid, wall radius 0.5 to
 50, first radial spacing 0.005 with the geometric ratio solved for the outer
 radius, dt=0.002, uniform start with a seeded +-1e-3 perturbation.  The Poisson
 iteration runs to the scaled-L1 tolerance 1e-10 under the reference's sweep cap
-NSWPP, set to 2000 so that every step does the same, reported, amount of line
-Gauss-Seidel work.  A step is one complete time step (Main.f90:48-114).
+NSWPP, set to 2048 so that every step does the same, reported, amount of line
+Gauss-Seidel work (both paths check the residual every 8 or 32 sweeps, which
+divide the cap).  A step is one complete time step (Main.f90:48-114).
 
 value: the mixed-precision path (FP32 zebra sweeps in FP64 refinement); the FP64
 path is timed in the same run.  e2e: the same metric through the C-ABI with the
@@ -31,7 +32,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = dict(name="cylinder2d-re200-thermal-512x384", n_theta=512, n_r=384, re=200.0, pr=0.71, dt=0.002,
-                resimax=1e-10, nswpp=2000, thermal=1, amp=1e-3, seed=0, dr1=0.005, r_out=50.0)
+                resimax=1e-10, nswpp=2048, thermal=1, amp=1e-3, seed=0, dr1=0.005, r_out=50.0,
+                res_every=8, refine_sweeps=32)
 METRIC = "Mcell-steps/s mixed vs FP64 GPU at <=1e-6 rel field error; adjoint/forward time"
 
 
@@ -63,7 +65,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -110,7 +112,7 @@ def make_ctx(w, precision, device, g, du, dv):
     from fvm_gb300 import capi
     p = capi.default_params(ni=g.ni, nj=g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], resimax=w["resimax"],
                             nswpp=w["nswpp"], thermal=w["thermal"], precision=precision,
-                            res_every=2, refine_sweeps=8, adi_refine=2, device=device)
+                            res_every=w["res_every"], refine_sweeps=w["refine_sweeps"], adi_refine=2, device=device)
     ctx = capi.Context(p)
     ctx.set_grid(g.xg, g.yg)
     ctx.init(du, dv)
@@ -151,37 +153,26 @@ def cpu_baseline(w, g, du, dv, steps=2):
                       f"serial restatement in the reference's lexicographic order, {dt:.1f} s"}
 
 
-def roofline_sweep(w, timing, peaks, mixed):
-    """Algorithmic bytes of the Poisson sweep kernels over the measured in-graph
-    spans.  FP32 sweep (per launch, one colour): per active cell RF, ANf, ASf,
-    invDf, faf, fbf read and DF written (28 B) plus the other colour's DF read
-    once (4 B): 32 B x active cells; the span's last launch also updates P
-    (read+write 16 B per cell) and reads the odd rows' DF (4 B per odd cell).
-    FP64 sweep: per active cell DIVDT, 4 cross weights, AN, AS, 3 factors (80 B)
-    read and P written (8 B), plus the other colour's P read (8 B, 16 B for the
-    colour that also reads the lagged input): 100 B x active cells on average."""
+def roofline_sweep(w, ms_per_launch, peaks, mixed):
+    """Roofline of the Poisson sweep kernel from its measured average launch time.
+    Algorithmic bytes per launch (one zebra colour = half the cells active):
+    FP32 sweep: per active cell RF, ANf, ASf, invDf, faf, fbf read and DF written
+    (28 B) plus the other colour's DF read once (4 B): 32 B x active cells.
+    FP64 sweep: per active cell DIVDT, 4 cross-term weights, AN, AS, 3 factors read
+    (80 B) and P written (8 B), plus the other colour's lagged P (8 B) and, for the
+    second colour, its new P (8 B): 100 B x active cells on average."""
     n_active = cells(w) // 2
-    launches = timing["sweep_span_launches"]
-    ms = timing["sweep_span_ms"]
-    if launches <= 0 or ms <= 0:
+    if not ms_per_launch or ms_per_launch <= 0:
         return None
-    if mixed:
-        per_span_launch = 32.0 * n_active
-        k = 8
-        span_bytes = (2 * k * per_span_launch + 16.0 * cells(w) + 4.0 * n_active) * (launches / (2 * k))
-        unit_bytes = span_bytes
-    else:
-        unit_bytes = 100.0 * n_active * launches
-    avg_ms = ms / launches
-    achieved = unit_bytes / (ms * 1e-3) / 1e9
+    per_launch = (32.0 if mixed else 100.0) * n_active
+    achieved = per_launch / (ms_per_launch * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs") if peaks else None
     peak_src = "measured" if peak else "fallback"
     if not peak:
         peak = 6800.0
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "kernel": "k_pois32" if mixed else "k_pois64",
-            "avg_launch_us": avg_ms * 1e3, "bytes_per_launch": unit_bytes / launches,
-            "peak_source": peak_src}
+            "avg_launch_us": ms_per_launch * 1e3, "bytes_per_launch": per_launch, "peak_source": peak_src}
 
 
 def run_ours(args):
@@ -202,7 +193,7 @@ def run_ours(args):
         peaks = json.load(open(pk))
 
     res = {}
-    for name, prec in (("fp64", capi.FP64), ("mixed", capi.MIXED)):
+    for name, prec in (("mixed", capi.MIXED), ("fp64", capi.FP64)):
         ctx = make_ctx(w, prec, local, g, du, dv)
         ext = torch.cuda.ExternalStream(ctx.stream_handle())
         ctx.step(args.warmup)
@@ -216,10 +207,14 @@ def run_ours(args):
         dist.barrier()
         ms_max = dist.max_over_ranks(ms, device="cuda")
         tm = ctx.timing()
+        # average launch time of the sweep kernel: CUDA events on the context's
+        # stream around a replay of 200 zebra sweeps of the same kernel on the
+        # state just reached (scratch arrays only)
+        sweep_ms, _ = ctx.time_sweeps(200)
         hist = ctx.history(1)
         fields = {nm: ctx.get(nm).copy() for nm in ("U", "V", "P", "T")}
         res[name] = dict(ms=ms_max, timing=tm, clocks=clocks, sweeps=hist[0]["sweeps"], fields=fields,
-                         cd=hist[0]["cd"], resid=hist[0]["resid"])
+                         cd=hist[0]["cd"], resid=hist[0]["resid"], sweep_ms=sweep_ms)
         ctx.close()
 
     # e2e through the C-ABI with host buffers (mixed path)
@@ -256,8 +251,8 @@ def run_ours(args):
     value = units / (res["mixed"]["ms"] * 1e-3) / 1e6
     fp64_value = units / (res["fp64"]["ms"] * 1e-3) / 1e6
     e2e_value = units / (e2e_ms * 1e-3) / 1e6
-    roof = roofline_sweep(w, res["mixed"]["timing"], peaks, True)
-    roof64 = roofline_sweep(w, res["fp64"]["timing"], peaks, False)
+    roof = roofline_sweep(w, res["mixed"]["sweep_ms"], peaks, True)
+    roof64 = roofline_sweep(w, res["fp64"]["sweep_ms"], peaks, False)
     traffic_file = os.path.join(ROOT, "profiles", "k_pois32_cylinder2d_512x384.json")
     if roof and os.path.exists(traffic_file):
         try:
@@ -273,8 +268,8 @@ def run_ours(args):
                    "cells": cells(w), "re": w["re"], "pr": w["pr"], "dt": w["dt"],
                    "poisson": f"zebra line GS to scaled-L1 {w['resimax']:g}, cap NSWPP={w['nswpp']}",
                    "sweeps_per_step": res["mixed"]["sweeps"], "precision": "mixed: FP32 zebra sweeps in FP64 "
-                   "refinement every 8 sweeps, FP32 predictor lines with 2 FP64 defect-correction passes; "
-                   "state, metrics and residuals FP64",
+                   f"refinement every {w['refine_sweeps']} sweeps, FP32 predictor lines with 2 FP64 "
+                   "defect-correction passes; state, metrics and residuals FP64",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "256 MiB buffer written between timed steps (outside the events)"},
         "fp64": {"value": fp64_value, "ms_per_step": res["fp64"]["ms"] / args.steps,
@@ -368,7 +363,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")

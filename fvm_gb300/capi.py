@@ -26,7 +26,7 @@ EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", 
            "fvm_set_time", "fvm_begin_step", "fvm_contra_vel", "fvm_nl", "fvm_dif", "fvm_p_source",
            "fvm_iter_u", "fvm_iter_v", "fvm_remove_grad", "fvm_iter_p", "fvm_correct", "fvm_iter_t",
            "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize", "fvm_get_stream",
-           "fvm_timing_reset", "fvm_get_timing"]
+           "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps"]
 
 
 class Params(ctypes.Structure):
@@ -36,7 +36,8 @@ class Params(ctypes.Structure):
                 ("tin", ctypes.c_double), ("t_wall", ctypes.c_double), ("resimax", ctypes.c_double),
                 ("nswpp", ctypes.c_int), ("precision", ctypes.c_int), ("thermal", ctypes.c_int),
                 ("iter_t_bug", ctypes.c_int), ("res_every", ctypes.c_int),
-                ("refine_sweeps", ctypes.c_int), ("adi_refine", ctypes.c_int), ("device", ctypes.c_int)]
+                ("refine_sweeps", ctypes.c_int), ("adi_refine", ctypes.c_int), ("device", ctypes.c_int),
+                ("poisson_groups", ctypes.c_int), ("poisson_host_loop", ctypes.c_int)]
 
 
 class Coeffs(ctypes.Structure):
@@ -107,6 +108,7 @@ def load(build_if_missing: bool = True):
     L.fvm_get_stream.argtypes = [V, ctypes.POINTER(ctypes.c_void_p)]
     L.fvm_timing_reset.argtypes = [V]
     L.fvm_get_timing.argtypes = [V, ctypes.POINTER(Timing)]
+    L.fvm_time_sweeps.argtypes = [V, ctypes.c_int, D, ctypes.POINTER(ctypes.c_longlong)]
     _lib = L
     return L
 
@@ -241,6 +243,12 @@ class Context:
 
     def timing_reset(self):
         self._ok(self.L.fvm_timing_reset(self.h))
+
+    def time_sweeps(self, sweeps=200):
+        ms = ctypes.c_double()
+        n = ctypes.c_longlong()
+        self._ok(self.L.fvm_time_sweeps(self.h, sweeps, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
 
     def timing(self) -> dict:
         t = Timing()

@@ -64,6 +64,8 @@ int fvm_default_params(fvm_params *p)
     p->refine_sweeps = 4;
     p->adi_refine = 2;
     p->device = 0;
+    p->poisson_groups = 16;
+    p->poisson_host_loop = 1;
     return FVM_OK;
 }
 
@@ -259,6 +261,13 @@ int fvm_timing_reset(fvm_ctx *c)
     if (!c) return FVM_ERR_ARG;
     c->tm = fvm_timing{};
     return FVM_OK;
+}
+
+int fvm_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches)
+{
+    READY();
+    if (sweeps < 1 || !ms_per_launch || !launches) return bad(c, "bad sweep timing arguments");
+    return fvm::run_time_sweeps(c, sweeps, ms_per_launch, launches);
 }
 
 int fvm_get_timing(fvm_ctx *c, fvm_timing *out)

@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/fvm.h"
@@ -14,16 +15,19 @@
 namespace fvm {
 
 constexpr int WARP = 32;
+constexpr int RES_CELLS = 2;   // cells per thread of the Poisson residual kernels
 
 // One set of constant tridiagonal factors for a family of lines (one line per
-// radial row j, or per circumferential column i).  Factors are stored
-// lane-interleaved: element e = lane*M + k of line L sits at L*32*M + k*32 + lane,
-// so every warp-wide load of one k is coalesced.  Padding elements (e >= n) have
-// zero factors and never influence real elements.
+// radial row j, or per circumferential column i), solved by groups of NW warps
+// (TG = 32*NW threads).  Factors are stored chunk-interleaved: element
+// e = t*M + k of line L sits at L*TG*M + k*TG + t, so every group-wide load of one
+// k is coalesced.  Padding elements (e >= n) have zero factors and never influence
+// real elements.
 struct LineSys {
     int lines = 0;     // number of lines
     int n = 0;         // unknowns per line
-    int M = 0;         // elements per lane (ceil(n/32))
+    int NW = 1;        // warps per line group
+    int M = 0;         // elements per thread (ceil(n/(32*NW)))
     int cyclic = 0;    // 1: periodic line solved by Sherman-Morrison
     double *invD = nullptr, *fa = nullptr, *fb = nullptr, *z = nullptr;  // FP64 factors
     float *invDf = nullptr, *faf = nullptr, *fbf = nullptr, *zf = nullptr; // FP32 copies
@@ -167,7 +171,9 @@ int run_calccoef(fvm_ctx *c, fvm_coeffs *out);
 int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out);
 double *array_by_name(fvm_ctx *c, const char *name);
 // mixed precision (fvm_mixed.cu)
-int mixed_poisson_capture(fvm_ctx *c, int outer);
+int mixed_poisson_body(fvm_ctx *c, cudaGraphConditionalHandle cond, int has_cond);
+int mixed_sweep_pair(fvm_ctx *c, int apply);
+int run_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches);
 int mixed_predictor_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi,
                            int colour, int refresh, const double *wallF, const double *farF);
 int mixed_predictor_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi,
@@ -217,23 +223,65 @@ __device__ __forceinline__ T shfl_down(T v, int s) { return __shfl_down_sync(0xf
 template <typename T>
 __device__ __forceinline__ T shfl_idx(T v, int s) { return __shfl_sync(0xffffffffu, v, s); }
 
+// ---------------------------------------------------------------------------------
+// Line solves by a group of NW warps (TG = 32*NW threads).  Thread t of the group
+// owns the chunk e = t*M .. t*M+M-1 of the line; the constant factors are stored
+// chunk-interleaved (element e = t*M + k at line_base + k*TG + t) so that every
+// factor load is coalesced.  Field arrays are read and written in the interleaved
+// ownership e = k*TG + t (coalesced along a Fortran row) and moved between the two
+// ownerships through shared memory.
+// ---------------------------------------------------------------------------------
+template <int NW>
+__device__ __forceinline__ void gsync()
+{
+    if (NW > 1) __syncthreads();
+    else __syncwarp();
+}
+
+__device__ __forceinline__ int spad(int e) { return e + (e >> 5); }
+
+template <typename T, int M, int NW>
+__device__ __forceinline__ void to_chunks(T (&v)[M], T *sm, int t)
+{
+    constexpr int TG = WARP * NW;
+#pragma unroll
+    for (int k = 0; k < M; k++) sm[spad(k * TG + t)] = v[k];
+    gsync<NW>();
+#pragma unroll
+    for (int k = 0; k < M; k++) v[k] = sm[spad(t * M + k)];
+    gsync<NW>();
+}
+
+template <typename T, int M, int NW>
+__device__ __forceinline__ void to_interleaved(T (&v)[M], T *sm, int t)
+{
+    constexpr int TG = WARP * NW;
+#pragma unroll
+    for (int k = 0; k < M; k++) sm[spad(t * M + k)] = v[k];
+    gsync<NW>();
+#pragma unroll
+    for (int k = 0; k < M; k++) v[k] = sm[spad(k * TG + t)];
+    gsync<NW>();
+}
+
 // Apply the precomputed LU factors of one line to the right-hand side held in
-// v[0..M-1] (lane owns elements lane*M .. lane*M+M-1), in place.
+// chunk ownership, in place:
 //   forward:  y_e = invD_e r_e + fa_e y_{e-1}
 //   backward: x_e = y_e + fb_e x_{e+1}
-// Each first-order recurrence is split into per-lane chunks, combined across the
-// warp by a Kogge-Stone scan of affine maps, and fixed up.  f* point at the line's
-// factor block (lane-interleaved).
-template <typename T, int M>
-__device__ __forceinline__ void line_apply(T (&v)[M], const T *__restrict__ invD,
-                                           const T *__restrict__ fa, const T *__restrict__ fb, int lane)
+// Each first-order recurrence runs sequentially inside a chunk, the chunks are
+// combined by a Kogge-Stone scan of affine maps across the warp and by a short
+// fold across the group's warps (xch: 2*NW values of shared scratch), then fixed up.
+template <typename T, int M, int NW>
+__device__ __forceinline__ void group_apply_r(T (&v)[M], const T (&fi)[M], const T (&fa)[M], const T (&fb)[M], int t,
+                                              T *xch)
 {
+    const int lane = t & (WARP - 1), wl = t / WARP;
     T gk[M];
     T y = T(0), g = T(1);
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        T a = fa[k * WARP + lane];
-        y = a * y + invD[k * WARP + lane] * v[k];
+        T a = fa[k];
+        y = a * y + fi[k] * v[k];
         v[k] = y;
         g = g * a;
         gk[k] = g;
@@ -244,15 +292,23 @@ __device__ __forceinline__ void line_apply(T (&v)[M], const T *__restrict__ invD
         T Gp = shfl_up(G, s), Yp = shfl_up(Y, s);
         if (lane >= s) { Y = Y + G * Yp; G = G * Gp; }
     }
-    T yin = shfl_up(Y, 1);
-    if (lane == 0) yin = T(0);
+    T yw = T(0);
+    if (NW > 1) {
+        if (lane == WARP - 1) { xch[2 * wl] = G; xch[2 * wl + 1] = Y; }
+        __syncthreads();
+        for (int w2 = 0; w2 < wl; w2++) yw = xch[2 * w2 + 1] + xch[2 * w2] * yw;
+        __syncthreads();
+    }
+    {
+        T Yp = shfl_up(Y, 1), Gp = shfl_up(G, 1);
+        T yin = (lane == 0) ? yw : Yp + Gp * yw;
 #pragma unroll
-    for (int k = 0; k < M; k++) v[k] = v[k] + gk[k] * yin;
-
+        for (int k = 0; k < M; k++) v[k] = v[k] + gk[k] * yin;
+    }
     T x = T(0), h = T(1);
 #pragma unroll
     for (int k = M - 1; k >= 0; k--) {
-        T b = fb[k * WARP + lane];
+        T b = fb[k];
         x = v[k] + b * x;
         v[k] = x;
         h = h * b;
@@ -264,27 +320,123 @@ __device__ __forceinline__ void line_apply(T (&v)[M], const T *__restrict__ invD
         T Hn = shfl_down(H, s), Xn = shfl_down(X, s);
         if (lane + s < WARP) { X = X + H * Xn; H = H * Hn; }
     }
-    T xin = shfl_down(X, 1);
-    if (lane == WARP - 1) xin = T(0);
+    T xw = T(0);
+    if (NW > 1) {
+        if (lane == 0) { xch[2 * wl] = H; xch[2 * wl + 1] = X; }
+        __syncthreads();
+        for (int w2 = NW - 1; w2 > wl; w2--) xw = xch[2 * w2 + 1] + xch[2 * w2] * xw;
+        __syncthreads();
+    }
+    {
+        T Xn = shfl_down(X, 1), Hn = shfl_down(H, 1);
+        T xin = (lane == WARP - 1) ? xw : Xn + Hn * xw;
 #pragma unroll
-    for (int k = 0; k < M; k++) v[k] = v[k] + gk[k] * xin;
+        for (int k = 0; k < M; k++) v[k] = v[k] + gk[k] * xin;
+    }
 }
 
-// Sherman-Morrison completion of a cyclic line after line_apply on the modified
-// matrix: x = y - ((y_1 + cv*y_n) * sinv) z.
-template <typename T, int M>
-__device__ __forceinline__ void line_cyclic_fix(T (&v)[M], const T *__restrict__ z, T cv, T sinv, int n, int lane)
+// Load the factors of one line (chunk ownership) into registers.
+template <typename T, int M, int NW>
+__device__ __forceinline__ void load_factors(T (&fi)[M], T (&fa)[M], T (&fb)[M], const T *__restrict__ invD,
+                                             const T *__restrict__ pa, const T *__restrict__ pb, int t)
 {
-    T y1 = shfl_idx(v[0], 0);
-    const int last = n - 1, ll = last / M, lk = last % M;
-    T yl = T(0);
+    constexpr int TG = WARP * NW;
 #pragma unroll
-    for (int k = 0; k < M; k++)
-        if (k == lk) yl = v[k];
-    yl = shfl_idx(yl, ll);
-    T w = (y1 + cv * yl) * sinv;
-#pragma unroll
-    for (int k = 0; k < M; k++) v[k] = v[k] - w * z[k * WARP + lane];
+    for (int k = 0; k < M; k++) {
+        fi[k] = invD[k * TG + t];
+        fa[k] = pa[k * TG + t];
+        fb[k] = pb[k * TG + t];
+    }
 }
+
+template <typename T, int M, int NW>
+__device__ __forceinline__ void group_apply(T (&v)[M], const T *__restrict__ invD, const T *__restrict__ fa,
+                                            const T *__restrict__ fb, int t, T *xch)
+{
+    T ri[M], ra[M], rb[M];
+    load_factors<T, M, NW>(ri, ra, rb, invD, fa, fb, t);
+    group_apply_r<T, M, NW>(v, ri, ra, rb, t, xch);
+}
+
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while its predecessor finishes; it must not read the
+// predecessor's results (or write anything the predecessor reads) before
+// griddep_wait().  griddep_launch() lets the successor start its own prologue.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Sherman-Morrison completion of a cyclic line after group_apply on the modified
+// matrix (chunk ownership): x = y - ((y_1 + cv*y_n) * sinv) z.  xch: 2 values.
+template <typename T, int M, int NW>
+__device__ __forceinline__ void group_cyclic_fix(T (&v)[M], const T *__restrict__ z, T cv, T sinv, int n, int t,
+                                                 T *xch)
+{
+    constexpr int TG = WARP * NW;
+    const int last = n - 1, tl = last / M, kl = last % M;
+    if (t == 0) xch[0] = v[0];
+    if (t == tl) {
+#pragma unroll
+        for (int k = 0; k < M; k++)
+            if (k == kl) xch[1] = v[k];
+    }
+    gsync<NW>();
+    T w = (xch[0] + cv * xch[1]) * sinv;
+    gsync<NW>();
+#pragma unroll
+    for (int k = 0; k < M; k++) v[k] = v[k] - w * z[k * TG + t];
+}
+
+// Group geometry of a line kernel launched with 128-thread blocks: 4/NW lines per
+// block; returns the group's line index and the thread index inside the group.
+template <int NW>
+__device__ __forceinline__ void group_of(int &gline, int &t, int &gib)
+{
+    constexpr int TG = WARP * NW;
+    gib = threadIdx.x / TG;
+    t = threadIdx.x % TG;
+    gline = blockIdx.x * (128 / TG) + gib;
+}
+
+// Host dispatch over the (elements per thread, warps per group) instantiations of a
+// line kernel: f(std::integral_constant<int,M>, std::integral_constant<int,NW>).
+template <typename F>
+inline bool dispatch_line(const LineSys &s, F &&f)
+{
+    using std::integral_constant;
+    switch (s.NW * 8 + s.M) {
+#define FVM_LCASE(NWV, MV) \
+    case NWV * 8 + MV: f(integral_constant<int, MV>(), integral_constant<int, NWV>()); return true;
+        FVM_LCASE(1, 1) FVM_LCASE(1, 2) FVM_LCASE(1, 3) FVM_LCASE(1, 4)
+        FVM_LCASE(2, 1) FVM_LCASE(2, 2) FVM_LCASE(2, 3) FVM_LCASE(2, 4)
+        FVM_LCASE(4, 1) FVM_LCASE(4, 2) FVM_LCASE(4, 3) FVM_LCASE(4, 4)
+#undef FVM_LCASE
+    default: return false;
+    }
+}
+
+// Launch with programmatic stream serialization (captured into graphs as
+// programmatic edges): the kernel may begin while the preceding kernel drains.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+// Blocks of 128 threads needed for `lines` line groups of NW warps.
+inline int line_blocks(int lines, int NW) { return (lines * NW + 3) / 4; }
+
+// Threads per line group for a line of n unknowns (elements per thread <= 4 for
+// n <= 512): one warp up to 128 unknowns, two up to 256, else four.
+inline int group_warps(int n) { return n <= 128 ? 1 : (n <= 256 ? 2 : 4); }
 
 }  // namespace fvm

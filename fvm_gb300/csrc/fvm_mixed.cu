@@ -21,16 +21,19 @@ namespace fvm {
 
 // FP64 residual of the current P, scaled-L1 norm, FP32 right-hand side of the
 // correction sweeps and zeroed correction.  The last block decides convergence.
-__global__ void __launch_bounds__(256) k_mres(Dev d)
+template <int HAS_COND>
+__global__ void __launch_bounds__(256) k_mres(Dev d, cudaGraphConditionalHandle cond)
 {
     __shared__ double sh[64];
     __shared__ bool last;
+    griddep_wait();
     if (d.pctl->done) return;
     const int it = d.pctl->niter;
     const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
     double ra = 0.0, pa = 0.0;
-    for (int q = 0; q < 4; q++) {
-        int e = blockIdx.x * 1024 + q * 256 + threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < RES_CELLS; q++) {
+        int e = (blockIdx.x * RES_CELLS + q) * 256 + threadIdx.x;
         if (e < total) {
             int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
             double su = d.DIVDT[c] - dd_p(d, d.P, i, j);
@@ -41,6 +44,7 @@ __global__ void __launch_bounds__(256) k_mres(Dev d)
             d.DF[c] = 0.0f;
         }
     }
+    griddep_launch();
     if (!grid_sum2(d, ra, pa, sh, last)) return;
     if (threadIdx.x == 0) {
         double resip = ra / pa;
@@ -48,6 +52,7 @@ __global__ void __launch_bounds__(256) k_mres(Dev d)
         if (it > 0 && !(resip > d.resimax && it < d.nswpp)) {
             d.pctl->done = 1;
             d.pctl->capped = (resip > d.resimax) ? 1 : 0;
+            if (HAS_COND) cudaGraphSetConditional(cond, 0);
         } else {
             d.pctl->niter = it + d.refine_sweeps;
         }
@@ -57,106 +62,105 @@ __global__ void __launch_bounds__(256) k_mres(Dev d)
 // One zebra colour of the FP32 correction sweep on radial rows.  With apply != 0
 // (the last colour-1 sweep of an outer iteration) the warp of even row j also adds
 // the correction of rows j and j-1 to P in FP64 and refreshes their BCP ghosts.
-template <int M>
-__global__ void __launch_bounds__(128) k_pois32(Dev d, int colour, int apply)
+template <int M, int NW>
+__global__ void __launch_bounds__(128) k_pois32(Dev d, int colour, int apply, int check_done)
 {
-    if (d.pctl->done) return;
-    const int lane = threadIdx.x & (WARP - 1);
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) / WARP;
-    if (w >= (d.NJ - 1) / 2) return;
-    const int j = 2 * w + 1 + colour;
+    constexpr int TG = WARP * NW, G = 4 / NW;
+    __shared__ float sm[G][TG * M + M * NW + 1];
+    __shared__ float xch[G][2 * NW];
+    int gl, t, gib;
+    group_of<NW>(gl, t, gib);
+    const bool active = gl < (d.NJ - 1) / 2;
+    const int j = active ? 2 * gl + 1 + colour : 1;
     const int jn = jwrap(d, j + 1), js = jwrap(d, j - 1);
     const LineSys &s = d.sP;
     const Coef &cf = d.cP;
     const int n = s.n;
+    // constants first: line factors and coupling coefficients
+    const size_t base = size_t(j - 1) * TG * M;
+    float fi[M], fa[M], fb[M], an[M], as[M];
+    load_factors<float, M, NW>(fi, fa, fb, s.invDf + base, s.faf + base, s.fbf + base, t);
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        int e = k * TG + t;
+        bool ok = active && e < n;
+        an[k] = ok ? cf.ANf[IDX(e + 1, j)] : 0.0f;
+        as[k] = ok ? cf.ASf[IDX(e + 1, j)] : 0.0f;
+    }
+    griddep_wait();
+    if (check_done && d.pctl->done) return;
     float v[M];
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
+        int e = k * TG + t;
         v[k] = 0.0f;
-        if (e < n) {
-            int i = e + 1, c = IDX(i, j);
-            v[k] = (cf.ANf[c] * d.DF[IDX(i, jn)] + cf.ASf[c] * d.DF[IDX(i, js)]) + d.RF[c];
+        if (active && e < n) {
+            int i = e + 1;
+            v[k] = (an[k] * d.DF[IDX(i, jn)] + as[k] * d.DF[IDX(i, js)]) + d.RF[IDX(i, j)];
         }
     }
-    const size_t base = size_t(j - 1) * WARP * M;
-    line_apply<float, M>(v, s.invDf + base, s.faf + base, s.fbf + base, lane);
+    griddep_launch();   // the next sweep may start its constant prologue now
+    to_chunks<float, M, NW>(v, sm[gib], t);
+    group_apply_r<float, M, NW>(v, fi, fa, fb, t, xch[gib]);
+    to_interleaved<float, M, NW>(v, sm[gib], t);
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
-        if (e < n) d.DF[IDX(e + 1, j)] = v[k];
+        int e = k * TG + t;
+        if (active && e < n) d.DF[IDX(e + 1, j)] = v[k];
     }
     if (!apply) return;
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
-        if (e < n) {
+        int e = k * TG + t;
+        if (active && e < n) {
             int i = e + 1;
             d.P[IDX(i, j)] += (double)v[k];
             d.P[IDX(i, j - 1)] += (double)d.DF[IDX(i, j - 1)];
         }
     }
-    __syncwarp();
-    refresh_row_ghosts<BCK_POISSON>(d, d.P, d.P, j, nullptr, nullptr, lane);
-    refresh_row_ghosts<BCK_POISSON>(d, d.P, d.P, j - 1, nullptr, nullptr, lane);
+    gsync<NW>();
+    if (active && t < WARP) {
+        refresh_row_ghosts<BCK_POISSON>(d, d.P, d.P, j, nullptr, nullptr, t);
+        refresh_row_ghosts<BCK_POISSON>(d, d.P, d.P, j - 1, nullptr, nullptr, t);
+    }
 }
 
-namespace {
-
-template <typename F>
-int dispatch_m(fvm_ctx *c, int M, F &&f)
+// One zebra sweep of the FP32 correction (both colours); apply != 0 also adds the
+// correction to P.  check_done is off when the pair is replayed for timing.
+static int sweep_pair(fvm_ctx *c, int apply, int check_done)
 {
-    switch (M) {
-    case 1: f(std::integral_constant<int, 1>()); break;
-    case 2: f(std::integral_constant<int, 2>()); break;
-    case 3: f(std::integral_constant<int, 3>()); break;
-    case 4: f(std::integral_constant<int, 4>()); break;
-    case 5: f(std::integral_constant<int, 5>()); break;
-    case 6: f(std::integral_constant<int, 6>()); break;
-    case 7: f(std::integral_constant<int, 7>()); break;
-    case 8: f(std::integral_constant<int, 8>()); break;
-    case 9: f(std::integral_constant<int, 9>()); break;
-    case 10: f(std::integral_constant<int, 10>()); break;
-    case 11: f(std::integral_constant<int, 11>()); break;
-    case 12: f(std::integral_constant<int, 12>()); break;
-    case 13: f(std::integral_constant<int, 13>()); break;
-    case 14: f(std::integral_constant<int, 14>()); break;
-    case 15: f(std::integral_constant<int, 15>()); break;
-    case 16: f(std::integral_constant<int, 16>()); break;
-    default:
+    Dev &d = c->d;
+    const int blocks = line_blocks((c->NJ - 1) / 2, d.sP.NW);
+    bool ok = dispatch_line(d.sP, [&](auto m, auto nw) {
+        auto k = k_pois32<decltype(m)::value, decltype(nw)::value>;
+        launch_pdl(k, dim3(blocks), dim3(128), c->stream, d, 0, 0, check_done);
+        launch_pdl(k, dim3(blocks), dim3(128), c->stream, d, 1, apply, check_done);
+    });
+    if (!ok) {
         c->err = "line length above 512 cells is not supported";
         return FVM_ERR_ARG;
     }
+    KCOUNT(c);
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
 
-}  // namespace
+int mixed_sweep_pair(fvm_ctx *c, int apply) { return sweep_pair(c, apply, 0); }
 
-int mixed_poisson_capture(fvm_ctx *c, int outer)
+// One outer iteration of the MIXED Poisson: FP64 residual (ends the device-side
+// loop when converged or capped), then refine_sweeps FP32 zebra sweeps, the last
+// of which adds the correction to P.
+int mixed_poisson_body(fvm_ctx *c, cudaGraphConditionalHandle cond, int has_cond)
 {
     Dev &d = c->d;
-    const int half = (c->NJ - 1) / 2;
-    const int blocks = (half * WARP + 127) / 128;
-    for (int o = 0; o < outer; o++) {
-        k_mres<<<c->nblk_res, 256, 0, c->stream>>>(d);
-        KCOUNT(c);
-        FVM_LAUNCH_CHECK(c);
-        if (o == 0) FVM_CUDA(c, cudaEventRecordWithFlags(c->ev_a, c->stream, cudaEventRecordExternal));
-        for (int s = 0; s < d.refine_sweeps; s++) {
-            const int apply = (s == d.refine_sweeps - 1);
-            int rc = dispatch_m(c, d.sP.M, [&](auto m) {
-                k_pois32<decltype(m)::value><<<blocks, 128, 0, c->stream>>>(d, 0, 0);
-                k_pois32<decltype(m)::value><<<blocks, 128, 0, c->stream>>>(d, 1, apply);
-                KCOUNT(c);
-                KCOUNT(c);
-            });
-            if (rc) return rc;
-        }
-        if (o == 0) {
-            FVM_CUDA(c, cudaEventRecordWithFlags(c->ev_b, c->stream, cudaEventRecordExternal));
-            c->span_launches = 2 * d.refine_sweeps;
-        }
+    if (has_cond) launch_pdl(k_mres<1>, dim3(c->nblk_res), dim3(256), c->stream, d, cond);
+    else launch_pdl(k_mres<0>, dim3(c->nblk_res), dim3(256), c->stream, d, cond);
+    KCOUNT(c);
+    FVM_LAUNCH_CHECK(c);
+    for (int s = 0; s < d.refine_sweeps; s++) {
+        int rc = sweep_pair(c, s == d.refine_sweeps - 1, 1);
+        if (rc) return rc;
     }
     return FVM_OK;
 }
@@ -165,27 +169,32 @@ int mixed_poisson_capture(fvm_ctx *c, int outer)
 // Predictor lines by defect correction
 // ---------------------------------------------------------------------------------
 // Radial row j: -AW x(i-1) + AP x(i) - AE x(i+1) = C (AW(1)=0, AE(NI-1)=0 folded).
-template <int M>
+// The line's FP64 values are staged in shared memory in natural order so that the
+// defect r = C - T x reads its neighbours there.
+template <int M, int NW>
 __global__ void __launch_bounds__(128) k_rad_dc(Dev d, LineSys s, Coef cf, const double *SU, double *phi, int colour,
                                                 int refresh, const double *wallF, const double *farF)
 {
-    const int lane = threadIdx.x & (WARP - 1);
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) / WARP;
-    if (w >= (d.NJ - 1) / 2) return;
-    const int j = 2 * w + 1 + colour;
+    constexpr int TG = WARP * NW, G = 4 / NW;
+    __shared__ double sx[G][TG * M + M * NW + 1];
+    __shared__ float sm[G][TG * M + M * NW + 1];
+    __shared__ float xch[G][2 * NW];
+    int gl, t, gib;
+    group_of<NW>(gl, t, gib);
+    const bool active = gl < (d.NJ - 1) / 2;
+    const int j = active ? 2 * gl + 1 + colour : 1;
     const int jn = jwrap(d, j + 1), js = jwrap(d, j - 1);
     const int n = s.n;
-    if (refresh) {
-        refresh_row_ghosts<BCK_DIRICHLET>(d, phi, phi, j, wallF, farF, lane);
-        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK_DIRICHLET>(d, phi, phi, j + 1, wallF, farF, lane);
-        __syncwarp();
+    if (active && refresh && t < WARP) {
+        refresh_row_ghosts<BCK_DIRICHLET>(d, phi, phi, j, wallF, farF, t);
+        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK_DIRICHLET>(d, phi, phi, j + 1, wallF, farF, t);
     }
     double C[M], x[M], ap[M], aw[M], ae[M];
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
+        int e = k * TG + t;
         C[k] = x[k] = ap[k] = aw[k] = ae[k] = 0.0;
-        if (e < n) {
+        if (active && e < n) {
             int i = e + 1, c = IDX(i, j);
             C[k] = (cf.AN[c] * phi[IDX(i, jn)] + cf.AS[c] * phi[IDX(i, js)]) + SU[c];
             x[k] = phi[c];
@@ -194,44 +203,54 @@ __global__ void __launch_bounds__(128) k_rad_dc(Dev d, LineSys s, Coef cf, const
             ae[k] = cf.AE[c];
         }
     }
-    const size_t base = size_t(j - 1) * WARP * M;
+    const size_t base = size_t(j - 1) * TG * M;
     for (int pass = 0; pass < d.adi_refine; pass++) {
-        double xl = shfl_up(x[M - 1], 1), xr = shfl_down(x[0], 1);
-        if (lane == 0) xl = 0.0;
-        if (lane == WARP - 1) xr = 0.0;
+#pragma unroll
+        for (int k = 0; k < M; k++) sx[gib][spad(k * TG + t)] = x[k];
+        gsync<NW>();
         float r[M];
 #pragma unroll
         for (int k = 0; k < M; k++) {
-            double xm = k > 0 ? x[k - 1] : xl, xp = k < M - 1 ? x[k + 1] : xr;
-            r[k] = (float)(C[k] - ((ap[k] * x[k] - aw[k] * xm) - ae[k] * xp));
+            int e = k * TG + t;
+            double xm = e > 0 ? sx[gib][spad(e - 1)] : 0.0;
+            double xp = e + 1 < n ? sx[gib][spad(e + 1)] : 0.0;
+            r[k] = (e < n) ? (float)(C[k] - ((ap[k] * x[k] - aw[k] * xm) - ae[k] * xp)) : 0.0f;
         }
-        line_apply<float, M>(r, s.invDf + base, s.faf + base, s.fbf + base, lane);
+        gsync<NW>();
+        to_chunks<float, M, NW>(r, sm[gib], t);
+        group_apply<float, M, NW>(r, s.invDf + base, s.faf + base, s.fbf + base, t, xch[gib]);
+        to_interleaved<float, M, NW>(r, sm[gib], t);
 #pragma unroll
         for (int k = 0; k < M; k++) x[k] += (double)r[k];
     }
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
-        if (e < n) phi[IDX(e + 1, j)] = x[k];
+        int e = k * TG + t;
+        if (active && e < n) phi[IDX(e + 1, j)] = x[k];
     }
 }
 
 // Circumferential column i, cyclic: -AS x(j-1) + AP x(j) - AN x(j+1) = C.
-template <int M>
+template <int M, int NW>
 __global__ void __launch_bounds__(128) k_theta_dc(Dev d, LineSys s, Coef cf, const double *SU, double *phi,
                                                   int colour, int ghosts, const double *wallF, const double *farF)
 {
-    const int lane = threadIdx.x & (WARP - 1);
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) / WARP;
-    const int i = 2 * w + 1 + colour;
-    if (i > d.NI - 1) return;
+    constexpr int TG = WARP * NW, G = 4 / NW;
+    __shared__ double sx[G][TG * M + M * NW + 1];
+    __shared__ float sm[G][TG * M + M * NW + 1];
+    __shared__ float xch[G][2 * NW];
+    int gl, t, gib;
+    group_of<NW>(gl, t, gib);
+    const int i0 = 2 * gl + 1 + colour;
+    const bool active = i0 <= d.NI - 1;
+    const int i = active ? i0 : 1;
     const int n = s.n;
     double C[M], x[M], ap[M], as[M], an[M];
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
+        int e = k * TG + t;
         C[k] = x[k] = ap[k] = as[k] = an[k] = 0.0;
-        if (e < n) {
+        if (active && e < n) {
             int c = IDX(i, e + 1);
             C[k] = (cf.AE[c] * phi[IDX(i + 1, e + 1)] + cf.AW[c] * phi[IDX(i - 1, e + 1)]) + SU[c];
             x[k] = phi[c];
@@ -240,35 +259,31 @@ __global__ void __launch_bounds__(128) k_theta_dc(Dev d, LineSys s, Coef cf, con
             an[k] = cf.AN[c];
         }
     }
-    const size_t base = size_t(i - 1) * WARP * M;
-    const int ll = (n - 1) / M, lk = (n - 1) % M;
+    const size_t base = size_t(i - 1) * TG * M;
     for (int pass = 0; pass < d.adi_refine; pass++) {
-        double xlast = 0.0;
 #pragma unroll
-        for (int k = 0; k < M; k++)
-            if (k == lk) xlast = x[k];
-        xlast = shfl_idx(xlast, ll);
-        const double xfirst = shfl_idx(x[0], 0);
-        double xl = shfl_up(x[M - 1], 1), xr = shfl_down(x[0], 1);
-        if (lane == 0) xl = xlast;
+        for (int k = 0; k < M; k++) sx[gib][spad(k * TG + t)] = x[k];
+        gsync<NW>();
         float r[M];
 #pragma unroll
         for (int k = 0; k < M; k++) {
-            int e = lane * M + k;
-            double xm = k > 0 ? x[k - 1] : xl;
-            double xp = (e == n - 1) ? xfirst : (k < M - 1 ? x[k + 1] : xr);
+            int e = k * TG + t;
+            double xm = sx[gib][spad(e > 0 ? e - 1 : n - 1)];
+            double xp = sx[gib][spad(e + 1 < n ? e + 1 : 0)];
             r[k] = (e < n) ? (float)(C[k] - ((ap[k] * x[k] - as[k] * xm) - an[k] * xp)) : 0.0f;
         }
-        line_apply<float, M>(r, s.invDf + base, s.faf + base, s.fbf + base, lane);
-        line_cyclic_fix<float, M>(r, s.zf + base, s.cvf[i - 1], s.sinvf[i - 1], n, lane);
+        gsync<NW>();
+        to_chunks<float, M, NW>(r, sm[gib], t);
+        group_apply<float, M, NW>(r, s.invDf + base, s.faf + base, s.fbf + base, t, xch[gib]);
+        group_cyclic_fix<float, M, NW>(r, s.zf + base, s.cvf[i - 1], s.sinvf[i - 1], n, t, xch[gib]);
+        to_interleaved<float, M, NW>(r, sm[gib], t);
 #pragma unroll
         for (int k = 0; k < M; k++) x[k] += (double)r[k];
     }
-    __syncwarp();
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
-        if (e < n) {
+        int e = k * TG + t;
+        if (active && e < n) {
             phi[IDX(i, e + 1)] = x[k];
             if (ghosts) ghost_dirichlet(d, phi, i, e + 1, x[k], wallF, farF);
         }
@@ -278,25 +293,37 @@ __global__ void __launch_bounds__(128) k_theta_dc(Dev d, LineSys s, Coef cf, con
 int mixed_predictor_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi, int colour,
                            int refresh, const double *wallF, const double *farF)
 {
-    const int half = (c->NJ - 1) / 2;
-    const int blocks = (half * WARP + 127) / 128;
     const Dev &d = c->d;
-    return dispatch_m(c, s.M, [&](auto m) {
-        k_rad_dc<decltype(m)::value><<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, refresh, wallF, farF);
-        KCOUNT(c);
+    const int blocks = line_blocks((c->NJ - 1) / 2, s.NW);
+    bool ok = dispatch_line(s, [&](auto m, auto nw) {
+        k_rad_dc<decltype(m)::value, decltype(nw)::value>
+            <<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, refresh, wallF, farF);
     });
+    if (!ok) {
+        c->err = "line length above 512 cells is not supported";
+        return FVM_ERR_ARG;
+    }
+    KCOUNT(c);
+    FVM_LAUNCH_CHECK(c);
+    return FVM_OK;
 }
 
 int mixed_predictor_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi, int colour,
                           int ghosts, const double *wallF, const double *farF)
 {
-    const int nl = (c->NI - 1 + 1 - colour) / 2;
-    const int blocks = (nl * WARP + 127) / 128;
     const Dev &d = c->d;
-    return dispatch_m(c, s.M, [&](auto m) {
-        k_theta_dc<decltype(m)::value><<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, ghosts, wallF, farF);
-        KCOUNT(c);
+    const int blocks = line_blocks((c->NI - 1 + 1 - colour) / 2, s.NW);
+    bool ok = dispatch_line(s, [&](auto m, auto nw) {
+        k_theta_dc<decltype(m)::value, decltype(nw)::value>
+            <<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, ghosts, wallF, farF);
     });
+    if (!ok) {
+        c->err = "line length above 512 cells is not supported";
+        return FVM_ERR_ARG;
+    }
+    KCOUNT(c);
+    FVM_LAUNCH_CHECK(c);
+    return FVM_OK;
 }
 
 }  // namespace fvm

@@ -30,9 +30,10 @@ void carve_sys(Bump &b, LineSys &s, int lines, int n, int cyclic)
 {
     s.lines = lines;
     s.n = n;
-    s.M = (n + WARP - 1) / WARP;
+    s.NW = group_warps(n);
+    s.M = (n + WARP * s.NW - 1) / (WARP * s.NW);
     s.cyclic = cyclic;
-    size_t cnt = size_t(lines) * WARP * s.M;
+    size_t cnt = size_t(lines) * WARP * s.NW * s.M;
     s.invD = b.take<double>(cnt);
     s.fa = b.take<double>(cnt);
     s.fb = b.take<double>(cnt);
@@ -132,7 +133,7 @@ int setup_allocate(fvm_ctx *c)
     d.iter_t_bug = c->p.iter_t_bug;
     d.adi_refine = c->p.adi_refine < 1 ? 1 : c->p.adi_refine;
     const int interior = (c->NI - 1) * (c->NJ - 1);
-    c->nblk_res = (interior + 1023) / 1024;   // residual kernels: 256 threads x 4 cells
+    c->nblk_res = (interior + 256 * RES_CELLS - 1) / (256 * RES_CELLS);   // residual kernels
     Bump probe{nullptr};
     carve(probe, c, c->nblk_res);
     c->slab_bytes = probe.off + 256;
@@ -361,10 +362,10 @@ __global__ void k_factor(Dev d, Coef cf, LineSys s, int circ)
 {
     int line = blockIdx.x * blockDim.x + threadIdx.x;
     if (line >= s.lines) return;
-    const int n = s.n, M = s.M;
-    const size_t base = size_t(line) * WARP * M;
+    const int n = s.n, M = s.M, TG = WARP * s.NW;
+    const size_t base = size_t(line) * TG * M;
     auto at = [&](int e) { return IDX(circ ? line + 1 : e + 1, circ ? e + 1 : line + 1); };
-    auto slot = [&](int e) { return base + size_t(e % M) * WARP + (e / M); };
+    auto slot = [&](int e) { return base + size_t(e % M) * TG + (e / M); };
     double gamma = 0.0, a1 = 0.0, cn = 0.0;
     if (circ) {
         gamma = -cf.AP[at(0)];
@@ -389,7 +390,7 @@ __global__ void k_factor(Dev d, Coef cf, LineSys s, int circ)
         s.fb[k] = -B;
         Bprev = B;
     }
-    for (int e = n; e < WARP * M; e++) {
+    for (int e = n; e < TG * M; e++) {
         size_t k = slot(e);
         s.invD[k] = 0.0;
         s.fa[k] = 0.0;
@@ -410,16 +411,16 @@ __global__ void k_factor(Dev d, Coef cf, LineSys s, int circ)
             x = s.z[k] + s.fb[k] * x;
             s.z[k] = x;
         }
-        for (int e = n; e < WARP * M; e++) s.z[slot(e)] = 0.0;
+        for (int e = n; e < TG * M; e++) s.z[slot(e)] = 0.0;
         double cv = a1 / gamma;
         double z1 = s.z[slot(0)], zn = s.z[slot(n - 1)];
         s.cv[line] = cv;
         s.sinv[line] = 1.0 / (1.0 + z1 + cv * zn);
         s.cvf[line] = (float)s.cv[line];
         s.sinvf[line] = (float)s.sinv[line];
-        for (int e = 0; e < WARP * M; e++) s.zf[slot(e)] = (float)s.z[slot(e)];
+        for (int e = 0; e < TG * M; e++) s.zf[slot(e)] = (float)s.z[slot(e)];
     }
-    for (int e = 0; e < WARP * M; e++) {
+    for (int e = 0; e < TG * M; e++) {
         size_t k = slot(e);
         s.invDf[k] = (float)s.invD[k];
         s.faf[k] = (float)s.fa[k];

@@ -236,42 +236,44 @@ __global__ void k_bcp_ghosts(Dev d)
 // ---------------------------------------------------------------------------------
 // Zebra radial-line sweep: lines j of one colour (colour 0: odd j) solve
 //   -AW x(i-1) + AP x(i) - AE x(i+1) = AN phi(i,j+1) + AS phi(i,j-1) + SU
-// with the neighbour rows read through periodic wrap (lisolv.f90:72-84,
-// iter_u.f90:52-64).  Colour 0 first refreshes the ghosts of its own row and of the
-// next (even) row from the pre-sweep values.
-template <int M, int BCK>
+// with the neighbour rows read through periodic wrap (iter_u.f90:52-64).
+// Colour 0 first refreshes the ghosts of its own row and of the next (even) row
+// from the pre-sweep values (the BCU call at iter_u.f90:48).
+template <int M, int NW, int BCK>
 __global__ void __launch_bounds__(128) k_radial(Dev d, LineSys s, Coef cf, const double *SU, double *phi, int colour,
-                                                int refresh, const double *wallF, const double *farF, int early_exit)
+                                                int refresh, const double *wallF, const double *farF)
 {
-    if (early_exit && d.pctl->done) return;
-    const int lane = threadIdx.x & (WARP - 1);
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) / WARP;
-    const int half = (d.NJ - 1) / 2;
-    if (w >= half) return;
-    const int j = 2 * w + 1 + colour;
+    constexpr int TG = WARP * NW, G = 4 / NW;
+    __shared__ double sm[G][TG * M + M * NW + 1];
+    __shared__ double xch[G][2 * NW];
+    int gl, t, gib;
+    group_of<NW>(gl, t, gib);
+    const bool active = gl < (d.NJ - 1) / 2;
+    const int j = active ? 2 * gl + 1 + colour : 1;
     const int jn = jwrap(d, j + 1), js = jwrap(d, j - 1);
     const int n = s.n;
-    if (refresh) {
-        refresh_row_ghosts<BCK>(d, phi, phi, j, wallF, farF, lane);
-        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK>(d, phi, phi, j + 1, wallF, farF, lane);
-        __syncwarp();
+    if (active && refresh && t < WARP) {
+        refresh_row_ghosts<BCK>(d, phi, phi, j, wallF, farF, t);
+        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK>(d, phi, phi, j + 1, wallF, farF, t);
     }
     double v[M];
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
+        int e = k * TG + t;
         v[k] = 0.0;
-        if (e < n) {
+        if (active && e < n) {
             int c = IDX(e + 1, j);
             v[k] = (cf.AN[c] * phi[IDX(e + 1, jn)] + cf.AS[c] * phi[IDX(e + 1, js)]) + SU[c];
         }
     }
-    const size_t base = size_t(j - 1) * WARP * M;
-    line_apply<double, M>(v, s.invD + base, s.fa + base, s.fb + base, lane);
+    to_chunks<double, M, NW>(v, sm[gib], t);
+    const size_t base = size_t(j - 1) * TG * M;
+    group_apply<double, M, NW>(v, s.invD + base, s.fa + base, s.fb + base, t, xch[gib]);
+    to_interleaved<double, M, NW>(v, sm[gib], t);
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
-        if (e < n) phi[IDX(e + 1, j)] = v[k];
+        int e = k * TG + t;
+        if (active && e < n) phi[IDX(e + 1, j)] = v[k];
     }
 }
 
@@ -280,33 +282,38 @@ __global__ void __launch_bounds__(128) k_radial(Dev d, LineSys s, Coef cf, const
 //   -AS x(j-1) + AP x(j) - AN x(j+1) = AE phi(i+1,j) + AW phi(i-1,j) + SU
 // (iter_u.f90:104-119 with the periodic coupling made implicit).  ghosts != 0 also
 // writes the BCT/BCU ghost cells derived from the new values.
-template <int M>
+template <int M, int NW>
 __global__ void __launch_bounds__(128) k_theta(Dev d, LineSys s, Coef cf, const double *SU, double *phi, int colour,
                                                int ghosts, const double *wallF, const double *farF)
 {
-    const int lane = threadIdx.x & (WARP - 1);
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) / WARP;
-    const int i = 2 * w + 1 + colour;
-    if (i > d.NI - 1) return;
+    constexpr int TG = WARP * NW, G = 4 / NW;
+    __shared__ double sm[G][TG * M + M * NW + 1];
+    __shared__ double xch[G][2 * NW];
+    int gl, t, gib;
+    group_of<NW>(gl, t, gib);
+    const int i0 = 2 * gl + 1 + colour;
+    const bool active = i0 <= d.NI - 1;
+    const int i = active ? i0 : 1;
     const int n = s.n;
     double v[M];
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
+        int e = k * TG + t;
         v[k] = 0.0;
-        if (e < n) {
+        if (active && e < n) {
             int c = IDX(i, e + 1);
             v[k] = (cf.AE[c] * phi[IDX(i + 1, e + 1)] + cf.AW[c] * phi[IDX(i - 1, e + 1)]) + SU[c];
         }
     }
-    const size_t base = size_t(i - 1) * WARP * M;
-    line_apply<double, M>(v, s.invD + base, s.fa + base, s.fb + base, lane);
-    line_cyclic_fix<double, M>(v, s.z + base, s.cv[i - 1], s.sinv[i - 1], n, lane);
-    __syncwarp();
+    to_chunks<double, M, NW>(v, sm[gib], t);
+    const size_t base = size_t(i - 1) * TG * M;
+    group_apply<double, M, NW>(v, s.invD + base, s.fa + base, s.fb + base, t, xch[gib]);
+    group_cyclic_fix<double, M, NW>(v, s.z + base, s.cv[i - 1], s.sinv[i - 1], n, t, xch[gib]);
+    to_interleaved<double, M, NW>(v, sm[gib], t);
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
-        if (e < n) {
+        int e = k * TG + t;
+        if (active && e < n) {
             phi[IDX(i, e + 1)] = v[k];
             if (ghosts) ghost_dirichlet(d, phi, i, e + 1, v[k], wallF, farF);
         }
@@ -322,56 +329,79 @@ __global__ void __launch_bounds__(128) k_theta(Dev d, LineSys s, Coef cf, const 
 // rows from Pin, colour 1 (even rows) from Pout, exactly the in-place zebra order,
 // while DD of both colours still sees P^(n-1) as the reference's lagged term does.
 // ---------------------------------------------------------------------------------
-template <int M>
-__global__ void __launch_bounds__(128) k_pois64(Dev d, const double *Pin, double *Pout, int colour)
+template <int M, int NW>
+__global__ void __launch_bounds__(128) k_pois64(Dev d, const double *Pin, double *Pout, int colour, int check_done)
 {
-    if (d.pctl->done) return;
-    const int lane = threadIdx.x & (WARP - 1);
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) / WARP;
-    if (w >= (d.NJ - 1) / 2) return;
-    const int j = 2 * w + 1 + colour;
+    constexpr int TG = WARP * NW, G = 4 / NW;
+    __shared__ double sm[G][TG * M + M * NW + 1];
+    __shared__ double xch[G][2 * NW];
+    int gl, t, gib;
+    group_of<NW>(gl, t, gib);
+    const bool active = gl < (d.NJ - 1) / 2;
+    const int j = active ? 2 * gl + 1 + colour : 1;
     const int jn = jwrap(d, j + 1), js = jwrap(d, j - 1);
     const LineSys &s = d.sP;
     const Coef &cf = d.cP;
     const int n = s.n;
-    if (colour == 0) {   // BCP of this iteration: ghosts of P^(n-1), stored with P^n
-        refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j, nullptr, nullptr, lane);
-        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j + 1, nullptr, nullptr, lane);
+    // constants first (factors, couplings, the step's source term)
+    const size_t base = size_t(j - 1) * TG * M;
+    double fi[M], fa[M], fb[M], an[M], as[M], dv[M];
+    load_factors<double, M, NW>(fi, fa, fb, s.invD + base, s.fa + base, s.fb + base, t);
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        int e = k * TG + t;
+        bool ok = active && e < n;
+        int c = IDX(e + 1, j);
+        an[k] = ok ? cf.AN[c] : 0.0;
+        as[k] = ok ? cf.AS[c] : 0.0;
+        dv[k] = ok ? d.DIVDT[c] : 0.0;
+    }
+    griddep_wait();
+    if (check_done && d.pctl->done) return;
+    if (active && colour == 0 && t < WARP) {   // BCP of this iteration: ghosts of P^(n-1), stored with P^n
+        refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j, nullptr, nullptr, t);
+        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j + 1, nullptr, nullptr, t);
     }
     const double *Pnb = colour ? Pout : Pin;
     double v[M];
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
+        int e = k * TG + t;
         v[k] = 0.0;
-        if (e < n) {
-            int i = e + 1, c = IDX(i, j);
-            double su = d.DIVDT[c] - dd_p(d, Pin, i, j);
-            v[k] = (cf.AN[c] * Pnb[IDX(i, jn)] + cf.AS[c] * Pnb[IDX(i, js)]) + su;
+        if (active && e < n) {
+            int i = e + 1;
+            double su = dv[k] - dd_p(d, Pin, i, j);
+            v[k] = (an[k] * Pnb[IDX(i, jn)] + as[k] * Pnb[IDX(i, js)]) + su;
         }
     }
-    const size_t base = size_t(j - 1) * WARP * M;
-    line_apply<double, M>(v, s.invD + base, s.fa + base, s.fb + base, lane);
+    griddep_launch();   // the next kernel may start its constant prologue now
+    to_chunks<double, M, NW>(v, sm[gib], t);
+    group_apply_r<double, M, NW>(v, fi, fa, fb, t, xch[gib]);
+    to_interleaved<double, M, NW>(v, sm[gib], t);
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        int e = lane * M + k;
-        if (e < n) Pout[IDX(e + 1, j)] = v[k];
+        int e = k * TG + t;
+        if (active && e < n) Pout[IDX(e + 1, j)] = v[k];
     }
 }
 
 // Residual after an even number of iterations: P^n in P, P^(n-1) in P2.  SU of the
 // last sweep is rebuilt from P^(n-1) (with its stored ghosts).  The last block
-// publishes the count and decides convergence (iter_p.f90:50-51).
-__global__ void __launch_bounds__(256) k_pres64(Dev d)
+// publishes the count and decides convergence (iter_p.f90:50-51); inside the
+// device-side loop it also ends the loop (cond != 0).
+template <int HAS_COND>
+__global__ void __launch_bounds__(256) k_pres64(Dev d, cudaGraphConditionalHandle cond)
 {
     __shared__ double sh[64];
     __shared__ bool last;
+    griddep_wait();
     if (d.pctl->done) return;
     const int it = d.pctl->niter + d.res_every;
     const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
     double ra = 0.0, pa = 0.0;
-    for (int q = 0; q < 4; q++) {
-        int e = blockIdx.x * 1024 + q * 256 + threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < RES_CELLS; q++) {
+        int e = (blockIdx.x * RES_CELLS + q) * 256 + threadIdx.x;
         if (e < total) {
             int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
             double su = d.DIVDT[c] - dd_p(d, d.P2, i, j);
@@ -380,6 +410,7 @@ __global__ void __launch_bounds__(256) k_pres64(Dev d)
             pa += fabs(d.cP.AP[c] * d.P[c]);
         }
     }
+    griddep_launch();
     if (!grid_sum2(d, ra, pa, sh, last)) return;
     if (threadIdx.x == 0) {
         double resip = ra / pa;
@@ -388,6 +419,7 @@ __global__ void __launch_bounds__(256) k_pres64(Dev d)
         if (!(resip > d.resimax && it < d.nswpp)) {
             d.pctl->done = 1;
             d.pctl->capped = (resip > d.resimax) ? 1 : 0;
+            if (HAS_COND) cudaGraphSetConditional(cond, 0);
         }
     }
 }
@@ -477,24 +509,19 @@ inline dim3 interior_grid(const fvm_ctx *c) { return dim3((c->NI - 1 + 127) / 12
 
 template <int BCK>
 int launch_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi, int colour,
-                  int refresh, const double *wallF, const double *farF, int early_exit)
+                  int refresh, const double *wallF, const double *farF, int /*unused*/)
 {
-    const int half = (c->NJ - 1) / 2;
-    const int blocks = (half * WARP + 127) / 128;
     const Dev &d = c->d;
-    switch (s.M) {
-#define CASE(MM)                                                                                   \
-    case MM:                                                                                       \
-        k_radial<MM, BCK><<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, refresh, wallF, farF, early_exit); \
-        KCOUNT(c);                                                                                 \
-        break;
-        CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
-        CASE(9) CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16)
-#undef CASE
-    default:
+    const int blocks = line_blocks((c->NJ - 1) / 2, s.NW);
+    bool ok = dispatch_line(s, [&](auto m, auto nw) {
+        k_radial<decltype(m)::value, decltype(nw)::value, BCK>
+            <<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, refresh, wallF, farF);
+    });
+    if (!ok) {
         c->err = "line length above 512 cells is not supported";
         return FVM_ERR_ARG;
     }
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -502,22 +529,17 @@ int launch_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU
 int launch_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi, int colour,
                  int ghosts, const double *wallF, const double *farF)
 {
-    const int nl = (c->NI - 1 + 1 - colour) / 2;
-    const int blocks = (nl * WARP + 127) / 128;
     const Dev &d = c->d;
-    switch (s.M) {
-#define CASE(MM)                                                                                   \
-    case MM:                                                                                       \
-        k_theta<MM><<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, ghosts, wallF, farF); \
-        KCOUNT(c);                                                                                 \
-        break;
-        CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
-        CASE(9) CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16)
-#undef CASE
-    default:
+    const int blocks = line_blocks((c->NI - 1 + 1 - colour) / 2, s.NW);
+    bool ok = dispatch_line(s, [&](auto m, auto nw) {
+        k_theta<decltype(m)::value, decltype(nw)::value>
+            <<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, ghosts, wallF, farF);
+    });
+    if (!ok) {
         c->err = "line length above 512 cells is not supported";
         return FVM_ERR_ARG;
     }
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
@@ -622,76 +644,106 @@ int run_remove_grad(fvm_ctx *c)
     return FVM_OK;
 }
 
-int launch_pois64(fvm_ctx *c, const double *Pin, double *Pout, int colour)
+int launch_pois64(fvm_ctx *c, const double *Pin, double *Pout, int colour, int check_done)
 {
-    const int half = (c->NJ - 1) / 2;
-    const int blocks = (half * WARP + 127) / 128;
     const Dev &d = c->d;
-    switch (d.sP.M) {
-#define CASE(MM)                                                                                   \
-    case MM:                                                                                       \
-        k_pois64<MM><<<blocks, 128, 0, c->stream>>>(d, Pin, Pout, colour);                         \
-        KCOUNT(c);                                                                                 \
-        break;
-        CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
-        CASE(9) CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16)
-#undef CASE
-    default:
+    const int blocks = line_blocks((c->NJ - 1) / 2, d.sP.NW);
+    bool ok = dispatch_line(d.sP, [&](auto m, auto nw) {
+        launch_pdl(k_pois64<decltype(m)::value, decltype(nw)::value>, dim3(blocks), dim3(128), c->stream, d, Pin,
+                   Pout, colour, check_done);
+    });
+    if (!ok) {
         c->err = "line length above 512 cells is not supported";
         return FVM_ERR_ARG;
     }
+    KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
 }
 
-// Capture `groups` residual intervals of the FP64 iteration into one graph:
-// res_every sweeps alternating P -> P2 -> P, then the residual.
-static int poisson64_capture(fvm_ctx *c, int groups)
+// One residual interval of the FP64 iteration: res_every sweeps alternating
+// P -> P2 -> P, then the residual (which ends the device-side loop when done).
+static int poisson64_body(fvm_ctx *c, cudaGraphConditionalHandle cond, int has_cond)
 {
     Dev &d = c->d;
-    int rc = FVM_OK;
-    for (int g = 0; g < groups && rc == FVM_OK; g++) {
-        if (g == 0) FVM_CUDA(c, cudaEventRecordWithFlags(c->ev_a, c->stream, cudaEventRecordExternal));
-        for (int it = 0; it < d.res_every && rc == FVM_OK; it++) {
-            const double *in = (it & 1) ? d.P2 : d.P;
-            double *out = (it & 1) ? d.P : d.P2;
-            rc = launch_pois64(c, in, out, 0);
-            if (rc == FVM_OK) rc = launch_pois64(c, in, out, 1);
-        }
-        if (g == 0) {
-            FVM_CUDA(c, cudaEventRecordWithFlags(c->ev_b, c->stream, cudaEventRecordExternal));
-            c->span_launches = 2 * d.res_every;
-        }
-        if (rc == FVM_OK) {
-            k_pres64<<<c->nblk_res, 256, 0, c->stream>>>(d);
-            KCOUNT(c);
-            FVM_LAUNCH_CHECK(c);
-        }
+    for (int it = 0; it < d.res_every; it++) {
+        const double *in = (it & 1) ? d.P2 : d.P;
+        double *out = (it & 1) ? d.P : d.P2;
+        RC(launch_pois64(c, in, out, 0, 1));
+        RC(launch_pois64(c, in, out, 1, 1));
     }
-    return rc;
+    if (has_cond) launch_pdl(k_pres64<1>, dim3(c->nblk_res), dim3(256), c->stream, d, cond);
+    else launch_pdl(k_pres64<0>, dim3(c->nblk_res), dim3(256), c->stream, d, cond);
+    KCOUNT(c);
+    FVM_LAUNCH_CHECK(c);
+    return FVM_OK;
+}
+
+// The whole Poisson iteration as one graph.  Device loop (default): a
+// while-conditional node whose body holds `groups` residual intervals; the residual
+// kernel clears the condition on convergence or at the sweep cap, so the loop ends
+// on the device without host synchronisation.  Host loop: the same body as a plain
+// graph, replayed by the host until the control block reports completion.
+static int body_groups(fvm_ctx *c, cudaGraphConditionalHandle h, int has_cond, int groups)
+{
+    const bool mixed = c->p.precision == FVM_MIXED;
+    for (int g = 0; g < groups; g++) RC(mixed ? mixed_poisson_body(c, h, has_cond) : poisson64_body(c, h, has_cond));
+    return FVM_OK;
 }
 
 static int poisson_graph(fvm_ctx *c)
 {
     if (c->pgraph) return FVM_OK;
-    Dev &d = c->d;
     const bool mixed = c->p.precision == FVM_MIXED;
-    const int per = mixed ? d.refine_sweeps : d.res_every;
-    int groups = (32 + per - 1) / per;   // about 32 sweeps per replay
+    const int per = mixed ? c->d.refine_sweeps : c->d.res_every;
+    int groups = c->p.poisson_groups > 0 ? c->p.poisson_groups : (32 + per - 1) / per;
     cudaGraph_t g = nullptr;
-    FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    c->capturing = true;
+    cudaError_t e;
     c->pgraph_kernels = 0;
-    int rc = mixed ? mixed_poisson_capture(c, groups) : poisson64_capture(c, groups);
-    c->capturing = false;
-    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-    if (rc) {
-        if (g) cudaGraphDestroy(g);
-        return rc;
-    }
-    if (e != cudaSuccess) {
-        c->err = std::string("Poisson graph capture: ") + cudaGetErrorString(e);
-        return FVM_ERR_CUDA;
+    if (c->p.poisson_host_loop) {
+        FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        c->capturing = true;
+        int rc = body_groups(c, 0, 0, groups);
+        c->capturing = false;
+        e = cudaStreamEndCapture(c->stream, &g);
+        if (rc || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (!rc) c->err = std::string("Poisson graph capture: ") + cudaGetErrorString(e);
+            return rc ? rc : FVM_ERR_CUDA;
+        }
+    } else {
+        FVM_CUDA(c, cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle h;
+        e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            c->err = std::string("Poisson loop node: ") + cudaGetErrorString(e);
+            return FVM_ERR_CUDA;
+        }
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            c->err = std::string("Poisson body capture: ") + cudaGetErrorString(e);
+            return FVM_ERR_CUDA;
+        }
+        c->capturing = true;
+        int rc = body_groups(c, h, 1, groups);
+        c->capturing = false;
+        cudaGraph_t body_out = body;
+        e = cudaStreamEndCapture(c->stream, &body_out);
+        if (rc || e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            if (!rc) c->err = std::string("Poisson body capture: ") + cudaGetErrorString(e);
+            return rc ? rc : FVM_ERR_CUDA;
+        }
     }
     e = cudaGraphInstantiate(&c->pgraph, g, 0);
     cudaGraphDestroy(g);
@@ -703,52 +755,114 @@ static int poisson_graph(fvm_ctx *c)
     return FVM_OK;
 }
 
-int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
+// Kernel launches of a finished Poisson loop (for the launch counter): whole
+// bodies are launched, their kernels returning early once converged.
+static long long poisson_loop_kernels(fvm_ctx *c, int niter)
+{
+    const int per = c->pgraph_batch;
+    const bool mixed = c->p.precision == FVM_MIXED;
+    long long bodies = (niter + (mixed ? 1 : 0) + per - 1) / per;
+    if (bodies < 1) bodies = 1;
+    return bodies * c->pgraph_kernels;
+}
+
+// Poisson phase of a step; with the device loop there is no host synchronisation
+// and the statistics stay on the device (CALCCOEF copies them with the
+// coefficients).
+static int iter_p_async(fvm_ctx *c)
 {
     Dev &d = c->d;
     k_contra_vel<<<interior_grid(c), 128, 0, c->stream>>>(d, 1);
     KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     RC(poisson_graph(c));
-    int status = FVM_OK;
-    // The device stops itself at the cap; the host bound only guards against a
-    // control block that never reports completion.
-    const long max_launches = (long)d.nswpp / c->pgraph_batch + 2;
-    const int per = c->p.precision == FVM_MIXED ? d.refine_sweeps : d.res_every;
-    int n0 = 0;
-    for (long launch = 0;; launch++) {
-        if (launch >= max_launches) {
-            c->err = "Poisson iteration did not report completion within the sweep cap";
-            return FVM_ERR_TIMEOUT;
-        }
+    if (!c->p.poisson_host_loop) {
         FVM_CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
-        c->tm.kernel_launches += c->pgraph_kernels;
-        FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
-        FVM_CUDA(c, cudaStreamSynchronize(c->stream));
-        // the span holds real sweeps only if the replay advanced past its first group
-        if (c->h_pctl->niter >= n0 + per) {
-            float ms = 0.f;
-            if (cudaEventElapsedTime(&ms, c->ev_a, c->ev_b) == cudaSuccess) {
-                c->tm.sweep_span_ms += ms;
-                c->tm.sweep_span_launches += c->span_launches;
-            } else {
-                (void)cudaGetLastError();   // a missing sample is not an error of the step
+    } else {
+        const long max_launches = (long)d.nswpp / c->pgraph_batch + 2;
+        for (long launch = 0;; launch++) {
+            if (launch >= max_launches) {
+                c->err = "Poisson iteration did not report completion within the sweep cap";
+                return FVM_ERR_TIMEOUT;
             }
+            FVM_CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
+            FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
+            FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+            if (c->h_pctl->done) break;
         }
-        n0 = c->h_pctl->niter;
-        if (c->h_pctl->done) break;
     }
+    k_bcp_ghosts<<<(c->NI + c->NJ + 127) / 128, 128, 0, c->stream>>>(d);
+    KCOUNT(c);
+    FVM_LAUNCH_CHECK(c);
+    return FVM_OK;
+}
+
+// Sweep kernels alone, for timing: `sweeps` zebra sweeps that touch only scratch
+// (FP64: P -> P2 both colours; MIXED: the FP32 correction without applying it),
+// replayed in a graph bracketed by CUDA events on the context's stream.
+static int time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches)
+{
+    Dev &d = c->d;
+    const bool mixed = c->p.precision == FVM_MIXED;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    int rc = FVM_OK;
+    for (int s = 0; s < sweeps && rc == FVM_OK; s++) {
+        if (mixed) rc = mixed_sweep_pair(c, 0);
+        else {
+            rc = launch_pois64(c, d.P, d.P2, 0, 0);
+            if (rc == FVM_OK) rc = launch_pois64(c, d.P, d.P2, 1, 0);
+        }
+    }
+    c->capturing = false;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (!rc) c->err = std::string("sweep timing capture: ") + cudaGetErrorString(e);
+        return rc ? rc : FVM_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->err = std::string("sweep timing instantiate: ") + cudaGetErrorString(e);
+        return FVM_ERR_CUDA;
+    }
+    FVM_CUDA(c, cudaGraphLaunch(ge, c->stream));   // warm
+    FVM_CUDA(c, cudaEventRecord(c->ev_a, c->stream));
+    FVM_CUDA(c, cudaGraphLaunch(ge, c->stream));
+    FVM_CUDA(c, cudaEventRecord(c->ev_b, c->stream));
+    FVM_CUDA(c, cudaEventSynchronize(c->ev_b));
+    float ms = 0.f;
+    FVM_CUDA(c, cudaEventElapsedTime(&ms, c->ev_a, c->ev_b));
+    cudaGraphExecDestroy(ge);
+    *launches = 2LL * sweeps;
+    *ms_per_launch = ms / (2.0 * sweeps);
+    c->tm.sweep_span_ms += ms;
+    c->tm.sweep_span_launches += 2LL * sweeps;
+    return FVM_OK;
+}
+
+int run_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches)
+{
+    return time_sweeps(c, sweeps, ms_per_launch, launches);
+}
+
+int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
+{
+    RC(iter_p_async(c));
+    FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, c->d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
+    FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->tm.kernel_launches += poisson_loop_kernels(c, c->h_pctl->niter);
     c->tm.sweeps += c->h_pctl->niter;
-    if (c->h_pctl->capped) status = FVM_ERR_NOCONV;
+    int status = c->h_pctl->capped ? FVM_ERR_NOCONV : FVM_OK;
     if (!std::isfinite(c->h_pctl->resip)) {
         c->err = "non-finite Poisson residual";
         status = FVM_ERR_NAN;
     }
     if (resid) *resid = c->h_pctl->resip;
     if (sweeps) *sweeps = c->h_pctl->niter;
-    k_bcp_ghosts<<<(c->NI + c->NJ + 127) / 128, 128, 0, c->stream>>>(d);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
     return status;
 }
 
@@ -805,13 +919,18 @@ int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out)
         RC(predictor_sweeps(c, FVM_FIELD_U));
         RC(predictor_sweeps(c, FVM_FIELD_V));
         RC(run_remove_grad(c));
-        int rc = run_iter_p(c, nullptr, nullptr);
-        if (rc == FVM_ERR_NOCONV) status = FVM_ERR_NOCONV;
-        else if (rc) return rc;
+        RC(iter_p_async(c));
         RC(run_correct(c));
         if (c->p.thermal) RC(predictor_sweeps(c, FVM_FIELD_T));
         fvm_coeffs co;
         RC(run_calccoef(c, &co));
+        c->tm.kernel_launches += poisson_loop_kernels(c, co.sweeps);
+        c->tm.sweeps += co.sweeps;
+        if (!std::isfinite(co.resid)) {
+            c->err = "non-finite Poisson residual";
+            return FVM_ERR_NAN;
+        }
+        if (co.resid > c->p.resimax) status = FVM_ERR_NOCONV;
         c->hist.push_back(co);
         c->tm.steps++;
         if (out) *out = co;

@@ -59,6 +59,9 @@ typedef struct fvm_params {
     int refine_sweeps;     /* MIXED: FP32 zebra sweeps per FP64 residual/refinement */
     int adi_refine;        /* MIXED: FP64 defect-correction passes per predictor line solve */
     int device;            /* CUDA device ordinal */
+    int poisson_groups;    /* residual intervals per Poisson graph body (0: about 32 sweeps) */
+    int poisson_host_loop; /* 1: the host replays the body until done (default; kernels stay visible
+                              to profilers); 0: the loop ends on the device in a graph while-node */
 } fvm_params;
 
 /* Per-step diagnostics of CALCCOEF (calccoef.f90:9-120) plus Poisson statistics. */
@@ -123,10 +126,9 @@ int fvm_synchronize(struct fvm_ctx *ctx);
 
 /* Instrumentation (no reference counterpart; used by benchmarks).  The CUDA
  * stream of the context (a cudaStream_t), and counters accumulated since the last
- * reset: CUDA-event time of spans that contain only Poisson sweep kernels inside
- * the replayed Poisson graph (one span per replay, around the first group of
- * sweeps), the number of sweep launches in those spans, every kernel the context
- * launched, Poisson sweeps and time steps. */
+ * reset: CUDA-event time of the sweep-kernel replays of fvm_time_sweeps and
+ * their launch count, every kernel the context launched (device-side loop
+ * iterations included), Poisson sweeps and time steps. */
 typedef struct fvm_timing {
     double sweep_span_ms;
     long long sweep_span_launches;
@@ -137,6 +139,10 @@ typedef struct fvm_timing {
 int fvm_get_stream(struct fvm_ctx *ctx, void **stream);
 int fvm_timing_reset(struct fvm_ctx *ctx);
 int fvm_get_timing(struct fvm_ctx *ctx, fvm_timing *out);
+/* Replays `sweeps` zebra sweeps of the Poisson sweep kernels of the context's
+ * precision (touching only scratch arrays, the state is unchanged) in a graph
+ * bracketed by CUDA events on the context's stream: average time per launch. */
+int fvm_time_sweeps(struct fvm_ctx *ctx, int sweeps, double *ms_per_launch, long long *launches);
 
 #ifdef __cplusplus
 }
