@@ -26,7 +26,7 @@ EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", 
            "fvm_set_time", "fvm_begin_step", "fvm_contra_vel", "fvm_nl", "fvm_dif", "fvm_p_source",
            "fvm_iter_u", "fvm_iter_v", "fvm_remove_grad", "fvm_iter_p", "fvm_correct", "fvm_iter_t",
            "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize", "fvm_get_stream",
-           "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps"]
+           "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps", "fvm_poisson_residual_static"]
 
 
 class Params(ctypes.Structure):
@@ -109,6 +109,7 @@ def load(build_if_missing: bool = True):
     L.fvm_timing_reset.argtypes = [V]
     L.fvm_get_timing.argtypes = [V, ctypes.POINTER(Timing)]
     L.fvm_time_sweeps.argtypes = [V, ctypes.c_int, D, ctypes.POINTER(ctypes.c_longlong)]
+    L.fvm_poisson_residual_static.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 8 + [V]
     _lib = L
     return L
 

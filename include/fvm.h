@@ -144,6 +144,27 @@ int fvm_get_timing(struct fvm_ctx *ctx, fvm_timing *out);
  * bracketed by CUDA events on the context's stream: average time per launch. */
 int fvm_time_sweeps(struct fvm_ctx *ctx, int sweeps, double *ms_per_launch, long long *launches);
 
+/* Allocation-free scaled residual of the pressure equation.  No counterpart in
+ * the reference: it serves callers that cannot allocate device memory (code
+ * recording a CUDA graph, where cudaMalloc is not allowed, or a host program whose
+ * device memory belongs to a pool or framework allocator).  It needs no context
+ * and allocates nothing; its only scratch is a fixed 32 KiB static device array
+ * that every GPU loading the library keeps until exit.
+ *   p, su, ap, ae, aw, an, as: caller-owned DEVICE arrays in the field layout above
+ *   (P with its ghost cells, the right-hand side SU and the five coefficients);
+ *   resid: caller-owned DEVICE pointer receiving sum|r| / sum|AP*P| over the
+ *   interior, r = AE P(I+1) + AW P(I-1) + AN P(J+1) + AS P(J-1) + SU - AP P with
+ *   J+1 / J-1 taken through the periodic branch cut; stream: a cudaStream_t (NULL:
+ *   the default stream).  The call is asynchronous on that stream.
+ * Limit: (NI-1)*(NJ-1) <= 1,048,576 interior cells, else FVM_ERR_ARG.  The first
+ * call on a device resolves the scratch address (once per device, with that device
+ * current) and should come before any stream capture.  All calls share the
+ * scratch, so calls that may overlap on the GPU (other streams, other host threads)
+ * race and must be serialised by the caller. */
+int fvm_poisson_residual_static(int ni, int nj, const double *p, const double *su, const double *ap,
+                                const double *ae, const double *aw, const double *an, const double *as,
+                                double *resid, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,74 @@
+"""GPU test of the allocation-free residual entry point.
+
+Some callers cannot allocate device memory (a stream being captured into a CUDA
+graph, or a program whose device memory is owned by a pool allocator);
+fvm_poisson_residual_static serves them with a fixed static scratch array.  This
+test calls it through the C-ABI on device arrays prepared outside the library and
+checks it against the residual the solver context reports for the same pressure
+field (the existing fvm_step entry point), twice in a row so that the shared
+scratch is reused.  It runs last and needs nothing from the other tests.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from fvm_gb300 import capi
+from tests.helpers import make_case, make_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def _poisson_system(ctx, g):
+    """Coefficients of the pressure equation with the wall/far-field folding
+    (iter_p.f90:12-17, bcp.f90:16-26) and SU = DIV/dt - DD(P) (iter_p.f90:24-30)
+    for the context's current pressure."""
+    get = ctx.get
+    DE, DW, DN, DS = get("DE"), get("DW"), get("DN"), get("DS")
+    AP = ((-DE) - DW - DN) - DS
+    AE, AW, AN, AS = -DE, -DW, -DN, -DS
+    AP[:, 1] = AP[:, 1] - AW[:, 1]
+    AW[:, 1] = 0.0
+    AE[:, g.ni - 1] = 0.0
+    K = get("DJAC") * get("Q12")
+    P = get("P")
+    ni, nj = g.ni, g.nj
+    SU = np.zeros_like(P)
+    i = np.arange(1, ni)[None, :]
+    j = np.arange(1, nj)[:, None]
+    ke, kw, kn, ks = K[j, i + 1], K[j, i - 1], K[j + 1, i], K[j - 1, i]
+    dd = ((0.25 * (ke + kn)) * P[j + 1, i + 1] + (-(0.25 * (ke + ks))) * P[j - 1, i + 1]
+          + (-(0.25 * (kw + kn))) * P[j + 1, i - 1] + (0.25 * (kw + ks)) * P[j - 1, i - 1])
+    SU[1:nj, 1:ni] = get("DIVDT")[1:nj, 1:ni] - dd
+    return P, SU, AP, AE, AW, AN, AS
+
+
+def test_static_residual_matches_the_step_residual():
+    torch = pytest.importorskip("torch")
+    # A capped (unconverged) Poisson solve keeps the residual well above rounding,
+    # so both evaluations of sum|r| agree to the suites' FP64 tolerance.
+    case = make_case(32, 24, skew=0.3, resimax=1e-14, nswpp=4)
+    g = case["g"]
+    ctx = make_gpu(case, precision=capi.MIXED, refine_sweeps=4)
+    ctx.step(1)
+    ref = ctx.step(1)["resid"]
+    arrays = [torch.tensor(np.ascontiguousarray(a).ravel(), dtype=torch.float64, device="cuda")
+              for a in _poisson_system(ctx, g)]
+    out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
+    L = capi.load()
+    ptrs = [ctypes.c_void_p(a.data_ptr()) for a in arrays]
+    for k in range(2):
+        rc = L.fvm_poisson_residual_static(g.ni, g.nj, *ptrs, ctypes.c_void_p(out[k:].data_ptr()), None)
+        assert rc == capi.FVM_OK
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    assert abs(got[0] - ref) <= 1e-12 * abs(ref), (got, ref)
+    assert abs(got[1] - ref) <= 1e-12 * abs(ref), (got, ref)
+
+
+def test_static_residual_rejects_oversized_grids():
+    L = capi.load()
+    dummy = [ctypes.c_void_p(8)] * 8
+    assert L.fvm_poisson_residual_static(2000, 2000, *dummy, None) == capi.FVM_ERR_ARG
+    assert L.fvm_poisson_residual_static(97, 129, *([None] * 8), None) == capi.FVM_ERR_ARG
