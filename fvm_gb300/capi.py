@@ -37,7 +37,8 @@ class Params(ctypes.Structure):
                 ("nswpp", ctypes.c_int), ("precision", ctypes.c_int), ("thermal", ctypes.c_int),
                 ("iter_t_bug", ctypes.c_int), ("res_every", ctypes.c_int),
                 ("refine_sweeps", ctypes.c_int), ("adi_refine", ctypes.c_int), ("device", ctypes.c_int),
-                ("poisson_groups", ctypes.c_int), ("poisson_host_loop", ctypes.c_int)]
+                ("poisson_groups", ctypes.c_int), ("poisson_host_loop", ctypes.c_int),
+                ("dd_positional", ctypes.c_int)]
 
 
 class Coeffs(ctypes.Structure):

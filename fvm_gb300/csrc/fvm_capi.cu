@@ -66,6 +66,7 @@ int fvm_default_params(fvm_params *p)
     p->device = 0;
     p->poisson_groups = 16;
     p->poisson_host_loop = 1;
+    p->dd_positional = 1;
     return FVM_OK;
 }
 

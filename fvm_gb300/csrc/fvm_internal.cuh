@@ -63,6 +63,7 @@ struct Dev {
     int nswpp;          // sweep cap, rounded up to a multiple of the residual interval
     int res_every;      // FP64: residual interval (even, >= 2)
     int iter_t_bug;
+    int dd_pos;         // 1: cell (i,j) takes the cross term of cell (i-1,j-1) in DIF / ITER_P
     int refine_sweeps;  // MIXED: FP32 sweeps per FP64 refinement
     int adi_refine;     // MIXED: defect-correction passes of a predictor line
     // geometry

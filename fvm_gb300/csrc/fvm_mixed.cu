@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(256) k_mres(Dev d, cudaGraphConditionalHandle 
         int e = (blockIdx.x * RES_CELLS + q) * 256 + threadIdx.x;
         if (e < total) {
             int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
-            double su = d.DIVDT[c] - dd_p(d, d.P, i, j);
+            double su = d.DIVDT[c] - dd_src(d, d.P, i, j);
             double r = pres_at(d, d.P, su, i, j);
             ra += fabs(r);
             pa += fabs(d.cP.AP[c] * d.P[c]);

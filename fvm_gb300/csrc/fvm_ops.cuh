@@ -33,10 +33,21 @@ __device__ __forceinline__ double cross_at(const Dev &d, const double *K, const 
     return 0.25 * (((t1 - t2) + t3) - t4);
 }
 
+// Cross term that DIF adds to cell (i,j).  DIF adds the whole array DD(0:NI,0:NJ)
+// to an expression over the section (1:NI-1,1:NJ-1) (dif.f90:15-23); compiled
+// code pairs the two element by element by position, so cell (i,j) receives the
+// term of cell (i-1,j-1), and zero on row 1 / column 1 (DD's row 0 and column 0
+// are never written).  dd_pos = 0 gives the cell's own term.
+__device__ __forceinline__ double dif_cross(const Dev &d, const double *in, int i, int j)
+{
+    if (!d.dd_pos) return cross_at(d, d.JQ12, in, i, j);
+    return (i > 1 && j > 1) ? cross_at(d, d.JQ12, in, i - 1, j - 1) : 0.0;
+}
+
 __device__ __forceinline__ double dif_at(const Dev &d, const double *in, int i, int j)
 {   // DIF (dif.f90:13-23)
     int c = IDX(i, j);
-    double dd = cross_at(d, d.JQ12, in, i, j);
+    double dd = dif_cross(d, in, i, j);
     double p = in[c];
     double a = d.DE[c] * (in[IDX(i + 1, j)] - p);
     double b = d.DW[c] * (in[IDX(i - 1, j)] - p);
@@ -136,6 +147,14 @@ __device__ __forceinline__ double dd_p(const Dev &d, const double *P, int i, int
     int c = IDX(i, j);
     return ((d.CNE[c] * P[IDX(i + 1, j + 1)] + d.CSE[c] * P[IDX(i + 1, j - 1)]) + d.CNW[c] * P[IDX(i - 1, j + 1)])
            + d.CSW[c] * P[IDX(i - 1, j - 1)];
+}
+
+// Cross term that ITER_P subtracts from the source of cell (i,j): the same
+// positional pairing as DIF (iter_p.f90:27-30), cell (i-1,j-1) or zero.
+__device__ __forceinline__ double dd_src(const Dev &d, const double *P, int i, int j)
+{
+    if (!d.dd_pos) return dd_p(d, P, i, j);
+    return (i > 1 && j > 1) ? dd_p(d, P, i - 1, j - 1) : 0.0;
 }
 
 // Deterministic block sum of two values (fixed shuffle tree, then warp 0).

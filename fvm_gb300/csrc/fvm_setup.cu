@@ -131,6 +131,7 @@ int setup_allocate(fvm_ctx *c)
     int k_ = c->p.precision == FVM_MIXED ? rs_ : re_;
     d.nswpp = ((c->p.nswpp + k_ - 1) / k_) * k_;
     d.iter_t_bug = c->p.iter_t_bug;
+    d.dd_pos = c->p.dd_positional ? 1 : 0;
     d.adi_refine = c->p.adi_refine < 1 ? 1 : c->p.adi_refine;
     const int interior = (c->NI - 1) * (c->NJ - 1);
     c->nblk_res = (interior + 256 * RES_CELLS - 1) / (256 * RES_CELLS);   // residual kernels

@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(128) k_pois64(Dev d, const double *Pin, double
         v[k] = 0.0;
         if (active && e < n) {
             int i = e + 1;
-            double su = dv[k] - dd_p(d, Pin, i, j);
+            double su = dv[k] - dd_src(d, Pin, i, j);
             v[k] = (an[k] * Pnb[IDX(i, jn)] + as[k] * Pnb[IDX(i, js)]) + su;
         }
     }
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(256) k_pres64(Dev d, cudaGraphConditionalHandl
         int e = (blockIdx.x * RES_CELLS + q) * 256 + threadIdx.x;
         if (e < total) {
             int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
-            double su = d.DIVDT[c] - dd_p(d, d.P2, i, j);
+            double su = d.DIVDT[c] - dd_src(d, d.P2, i, j);
             double r = pres_at(d, d.P, su, i, j);
             ra += fabs(r);
             pa += fabs(d.cP.AP[c] * d.P[c]);

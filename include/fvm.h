@@ -62,6 +62,9 @@ typedef struct fvm_params {
     int poisson_groups;    /* residual intervals per Poisson graph body (0: about 32 sweeps) */
     int poisson_host_loop; /* 1: the host replays the body until done (default; kernels stay visible
                               to profilers); 0: the loop ends on the device in a graph while-node */
+    int dd_positional;     /* 1 (default): DIF and ITER_P add the cross term of cell (I-1,J-1) to
+                              cell (I,J), zero on row/column 1, as the reference's whole-array DD
+                              operand evaluates (dif.f90:15-23, iter_p.f90:27-30); 0: cell (I,J) */
 } fvm_params;
 
 /* Per-step diagnostics of CALCCOEF (calccoef.f90:9-120) plus Poisson statistics. */

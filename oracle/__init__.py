@@ -23,7 +23,7 @@ class Params(ctypes.Structure):
                 ("vel_rot", ctypes.c_double), ("uin", ctypes.c_double), ("vin", ctypes.c_double),
                 ("tin", ctypes.c_double), ("t_wall", ctypes.c_double), ("resimax", ctypes.c_double),
                 ("nswpp", ctypes.c_int), ("order", ctypes.c_int), ("iter_t_bug", ctypes.c_int),
-                ("thermal", ctypes.c_int), ("res_every", ctypes.c_int)]
+                ("thermal", ctypes.c_int), ("res_every", ctypes.c_int), ("dd_positional", ctypes.c_int)]
 
 
 class Coeffs(ctypes.Structure):
@@ -82,11 +82,12 @@ class Oracle:
 
     def __init__(self, ni, nj, re=100.0, pr=0.71, dt=0.005, vel_rot=0.0, order=GPU,
                  resimax=1e-10, nswpp=100000, thermal=True, iter_t_bug=True, res_every=1,
-                 uin=1.0, vin=0.0, tin=0.0, t_wall=1.0):
+                 uin=1.0, vin=0.0, tin=0.0, t_wall=1.0, dd_positional=True):
         self.ni, self.nj = ni, nj
         p = Params(ni=ni, nj=nj, re=re, pr=pr, dt=dt, vel_rot=vel_rot, uin=uin, vin=vin, tin=tin,
                    t_wall=t_wall, resimax=resimax, nswpp=nswpp, order=order,
-                   iter_t_bug=int(iter_t_bug), thermal=int(thermal), res_every=res_every)
+                   iter_t_bug=int(iter_t_bug), thermal=int(thermal), res_every=res_every,
+                   dd_positional=int(dd_positional))
         self._p = p
         self._h = lib().orc_create(ctypes.byref(p))
         if not self._h:

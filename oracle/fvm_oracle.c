@@ -389,6 +389,17 @@ static void dif_diagonal(orc *o, const double *f, double *out)
         }
 }
 
+/* Cell whose cross term DIF and ITER_P add to cell (i,j).  Both routines add the
+ * whole array DD(0:NI,0:NJ) to an expression over the interior section
+ * (1:NI-1,1:NJ-1) (dif.f90:15-23, iter_p.f90:27-30).  The shapes do not conform;
+ * compiled code evaluates the sum element by element by position, so interior
+ * cell (i,j) receives DD(i-1,j-1) -- zero on row 0 and column 0, which no routine
+ * writes.  dd_positional=0 selects the cell's own term instead. */
+static inline int dd_at(const orc *o, int i, int j)
+{
+    return o->p.dd_positional ? ID(i - 1, j - 1) : ID(i, j);
+}
+
 /* DIF (dif.f90:13-23) */
 static void dif(orc *o, const double *in, double *out)
 {
@@ -401,7 +412,7 @@ static void dif(orc *o, const double *in, double *out)
             double b = o->DW[c] * (in[ID(i - 1, j)] - in[c]);
             double d = o->DN[c] * (in[ID(i, j + 1)] - in[c]);
             double e = o->DS[c] * (in[ID(i, j - 1)] - in[c]);
-            out[c] = 1.0 * ((((a + b) + d) + e) + o->DD[c]);
+            out[c] = 1.0 * ((((a + b) + d) + e) + o->DD[dd_at(o, i, j)]);
         }
 }
 
@@ -642,7 +653,7 @@ static int iter_p(orc *o)
         for (int j = 1; j <= NJ - 1; j++)
             for (int i = 1; i <= NI - 1; i++) {
                 int c = ID(i, j);
-                o->SU[c] = rdt * (((o->UE[c] - o->UW[c]) + o->VN[c]) - o->VS[c]) - o->DD[c];
+                o->SU[c] = rdt * (((o->UE[c] - o->UW[c]) + o->VN[c]) - o->VS[c]) - o->DD[dd_at(o, i, j)];
             }
         bcp(o);
         sweep_radial(o, o->P);

@@ -7,8 +7,12 @@
  *
  * Reference: cylinder/cylinder_v3.0.3_AF_original 4step_face_nl/ (Fortran 90).
  * The reference cannot be compiled here (no Fortran compiler on either machine)
- * and ships no tests or golden vectors: parity unpinned by the reference's own
- * tests.
+ * and ships no tests or golden vectors.  The restatement is pinned instead by
+ * executing the reference's own source files: tests/golden/make_golden.py runs
+ * them through a Fortran-subset interpreter (tests/golden/ftn_interp.py) on small
+ * grids and commits U, V, P, T, NLX, NLY, ADV and every coefficient record as
+ * fixtures; ORC_FAITHFUL with dd_positional=1 reproduces them (tests compare at
+ * 1e-12 relative L2 and 1e-11 on the coefficients).
  *
  * Arrays follow the reference layout: Fortran order (0:NI, 0:NJ), element
  * (i, j) at i + (NI+1)*j, I radial (wall ghost i=0, far-field ghost i=NI),
@@ -44,6 +48,10 @@ typedef struct {
     int iter_t_bug;      /* 1: second-sweep cross term of ITER_T built from V (iter_T.f90:89-95) */
     int thermal;         /* 1: advance the passive temperature (ITER_T + BCT) */
     int res_every;       /* ORC_GPU: residual evaluated every k-th sweep (>=1) */
+    int dd_positional;   /* 1: DIF and ITER_P add the cross term of cell (I-1,J-1), as the
+                            reference's whole-array DD operand in an interior-section
+                            expression evaluates (dif.f90:15-23, iter_p.f90:27-30);
+                            0: the cross term of cell (I,J) */
 } orc_params;
 
 typedef struct {

@@ -128,6 +128,10 @@ def test_iter_t_bug_switch_changes_only_temperature():
     assert not np.array_equal(a.array("T"), b.array("T"))
 
 
+# record layout of the coefficient file written by CALCCOEF
+GOLD_COEFFS = ("time", "nu", "cd", "cl", "cpb", "cd_p", "cd_v", "cl_p", "cl_v", "cfl")
+
+
 def _golden_cases():
     path = os.path.join(GOLD, "manifest.json")
     if not os.path.exists(path):
@@ -146,9 +150,17 @@ def test_oracle_against_golden_fixtures(entry):
                       thermal=True, iter_t_bug=True)
     o.set_grid(g.xg, g.yg)
     o.init(du, dv)
-    o.step(entry["steps"])
+    recs = []
+    for _ in range(entry["steps"]):
+        o.step(1)
+        c = o.coeffs()
+        recs.append([c[k] for k in GOLD_COEFFS])
     tol = entry["tol"]
     for nm in entry["fields"]:
         ref = data[nm]
         got = o.array(nm)
         assert rel_l2(got, ref) <= tol, nm
+    # one NU_CD_CL.PLT record per step (calccoef.f90:122-123)
+    ref = data["COEFFS"]
+    assert ref.shape == (entry["steps"], len(GOLD_COEFFS))
+    np.testing.assert_allclose(np.array(recs), ref, rtol=1e-11, atol=1e-11)

@@ -21,7 +21,8 @@ pytestmark = pytest.mark.gpu
 
 def _poisson_system(ctx, g):
     """Coefficients of the pressure equation with the wall/far-field folding
-    (iter_p.f90:12-17, bcp.f90:16-26) and SU = DIV/dt - DD(P) (iter_p.f90:24-30)
+    (iter_p.f90:12-17, bcp.f90:16-26) and SU = DIV/dt - DD(P) (iter_p.f90:24-30),
+    DD paired by position
     for the context's current pressure."""
     get = ctx.get
     DE, DW, DN, DS = get("DE"), get("DW"), get("DN"), get("DS")
@@ -39,7 +40,11 @@ def _poisson_system(ctx, g):
     ke, kw, kn, ks = K[j, i + 1], K[j, i - 1], K[j + 1, i], K[j - 1, i]
     dd = ((0.25 * (ke + kn)) * P[j + 1, i + 1] + (-(0.25 * (ke + ks))) * P[j - 1, i + 1]
           + (-(0.25 * (kw + kn))) * P[j + 1, i - 1] + (0.25 * (kw + ks)) * P[j - 1, i - 1])
-    SU[1:nj, 1:ni] = get("DIVDT")[1:nj, 1:ni] - dd
+    # cell (I,J) takes the cross term of cell (I-1,J-1), zero on row/column 1
+    # (the positional whole-array DD of iter_p.f90:27-30)
+    dds = np.zeros_like(dd)
+    dds[1:, 1:] = dd[:-1, :-1]
+    SU[1:nj, 1:ni] = get("DIVDT")[1:nj, 1:ni] - dds
     return P, SU, AP, AE, AW, AN, AS
 
 
