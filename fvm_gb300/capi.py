@@ -26,7 +26,10 @@ EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", 
            "fvm_set_time", "fvm_begin_step", "fvm_contra_vel", "fvm_nl", "fvm_dif", "fvm_p_source",
            "fvm_iter_u", "fvm_iter_v", "fvm_remove_grad", "fvm_iter_p", "fvm_correct", "fvm_iter_t",
            "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize", "fvm_get_stream",
-           "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps", "fvm_poisson_residual_static"]
+           "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps", "fvm_poisson_residual_static",
+           "fvm_batch_create", "fvm_batch_destroy", "fvm_batch_last_error", "fvm_batch_case",
+           "fvm_batch_tiles", "fvm_batch_set_tiles", "fvm_batch_autotune", "fvm_batch_time_sweeps",
+           "fvm_batch_step", "fvm_batch_get_timing"]
 
 
 class Params(ctypes.Structure):
@@ -38,7 +41,9 @@ class Params(ctypes.Structure):
                 ("iter_t_bug", ctypes.c_int), ("res_every", ctypes.c_int),
                 ("refine_sweeps", ctypes.c_int), ("adi_refine", ctypes.c_int), ("device", ctypes.c_int),
                 ("poisson_groups", ctypes.c_int), ("poisson_host_loop", ctypes.c_int),
-                ("dd_positional", ctypes.c_int)]
+                ("dd_positional", ctypes.c_int),
+                ("tile_r_warps", ctypes.c_int), ("tile_r_m", ctypes.c_int),
+                ("tile_t_warps", ctypes.c_int), ("tile_t_m", ctypes.c_int)]
 
 
 class Coeffs(ctypes.Structure):
@@ -111,6 +116,18 @@ def load(build_if_missing: bool = True):
     L.fvm_get_timing.argtypes = [V, ctypes.POINTER(Timing)]
     L.fvm_time_sweeps.argtypes = [V, ctypes.c_int, D, ctypes.POINTER(ctypes.c_longlong)]
     L.fvm_poisson_residual_static.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 8 + [V]
+    I = ctypes.POINTER(ctypes.c_int)
+    L.fvm_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(Params), ctypes.POINTER(V)]
+    L.fvm_batch_destroy.argtypes = [V]
+    L.fvm_batch_last_error.argtypes = [V]
+    L.fvm_batch_last_error.restype = ctypes.c_char_p
+    L.fvm_batch_case.argtypes = [V, ctypes.c_int, ctypes.POINTER(V)]
+    L.fvm_batch_tiles.argtypes = [V, I]
+    L.fvm_batch_set_tiles.argtypes = [V, I]
+    L.fvm_batch_autotune.argtypes = [V, ctypes.c_int, I, D]
+    L.fvm_batch_time_sweeps.argtypes = [V, ctypes.c_int, D]
+    L.fvm_batch_step.argtypes = [V, ctypes.c_int, ctypes.POINTER(Coeffs)]
+    L.fvm_batch_get_timing.argtypes = [V, ctypes.POINTER(Timing)]
     _lib = L
     return L
 
@@ -142,11 +159,15 @@ class Context:
     """One solver context (one CUDA stream on one GPU).  Field arrays are numpy
     arrays shaped (NJ+1, NI+1): a[j, i] is the reference's (I, J)."""
 
-    def __init__(self, params: Params):
+    def __init__(self, params: Params, _handle=None, _owner=None):
         self.L = load()
         self.p = params
         self.ni, self.nj = params.ni, params.nj
         self.n = (self.ni + 1) * (self.nj + 1)
+        self._owner = _owner          # a Batch owns the contexts of its cases
+        if _handle is not None:
+            self.h = _handle
+            return
         h = ctypes.c_void_p()
         rc = self.L.fvm_create(ctypes.byref(params), ctypes.byref(h))
         if rc != FVM_OK:
@@ -154,9 +175,9 @@ class Context:
         self.h = h
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and self._owner is None:
             self.L.fvm_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -267,3 +288,81 @@ class Context:
         P = ctypes.POINTER(ctypes.c_double)
         args = [ctypes.cast(p, P) if p else None for p in ptrs]
         self._ok(self.L.fvm_download_state(self.h, *args))
+
+
+class Batch:
+    """Independent cases advanced together (fvm_batch_*).  cases[k] is the
+    Context of case k (owned by the batch): set its grid and initial state with the
+    Context methods, then step the batch."""
+
+    def __init__(self, params_list):
+        self.L = load()
+        self.params = list(params_list)
+        arr = (Params * len(self.params))(*self.params)
+        h = ctypes.c_void_p()
+        rc = self.L.fvm_batch_create(len(self.params), arr, ctypes.byref(h))
+        if rc != FVM_OK:
+            raise FvmError(rc, "fvm_batch_create failed (run options and tiles must agree across cases)")
+        self.h = h
+        self.cases = []
+        for k, p in enumerate(self.params):
+            ch = ctypes.c_void_p()
+            self._ok(self.L.fvm_batch_case(self.h, k, ctypes.byref(ch)))
+            q = Params()
+            ctypes.pointer(q)[0] = p
+            self.cases.append(Context(q, _handle=ch, _owner=self))
+
+    def __len__(self):
+        return len(self.cases)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for c in self.cases:
+                c.h = None
+            self.L.fvm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc, allow=()):
+        if rc != FVM_OK and rc not in allow:
+            raise FvmError(rc, self.L.fvm_batch_last_error(self.h).decode())
+        return rc
+
+    def tiles(self):
+        t = (ctypes.c_int * 4)()
+        self._ok(self.L.fvm_batch_tiles(self.h, t))
+        return tuple(t)
+
+    def set_tiles(self, tiles):
+        t = (ctypes.c_int * 4)(*tiles)
+        self._ok(self.L.fvm_batch_set_tiles(self.h, t))
+
+    def autotune(self, sweeps=50):
+        """Times the candidate line tiles on this batch and keeps the fastest;
+        returns (tiles, ms per sweep of the radial and circumferential families)."""
+        t = (ctypes.c_int * 4)()
+        ms = (ctypes.c_double * 2)()
+        self._ok(self.L.fvm_batch_autotune(self.h, sweeps, t, ms))
+        return tuple(t), (ms[0], ms[1])
+
+    def time_sweeps(self, sweeps=100):
+        ms = ctypes.c_double()
+        self._ok(self.L.fvm_batch_time_sweeps(self.h, sweeps, ctypes.byref(ms)))
+        return ms.value
+
+    def step(self, n=1):
+        """n steps of every case; returns records[s][k] (dicts)."""
+        k = len(self.cases)
+        arr = (Coeffs * (n * k))()
+        self._ok(self.L.fvm_batch_step(self.h, n, arr), allow=(FVM_ERR_NOCONV,))
+        return [[arr[s * k + j].as_dict() for j in range(k)] for s in range(n)]
+
+    def timing(self) -> dict:
+        t = Timing()
+        self._ok(self.L.fvm_batch_get_timing(self.h, ctypes.byref(t)))
+        return t.as_dict()

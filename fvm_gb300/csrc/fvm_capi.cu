@@ -34,6 +34,17 @@ int check_params(const fvm_params *p, std::string &why)
     if (!(p->dt > 0.0) || !(p->re > 0.0) || !(p->pr > 0.0)) { why = "dt, re and pr must be positive"; return FVM_ERR_ARG; }
     if (!(p->resimax >= 0.0) || p->nswpp < 1) { why = "resimax must be >= 0 and nswpp >= 1"; return FVM_ERR_ARG; }
     if (p->precision != FVM_FP64 && p->precision != FVM_MIXED) { why = "unknown precision"; return FVM_ERR_ARG; }
+    auto tile_ok = [&](int nw, int m, int n, const char *fam) {
+        if (nw == 0 && m == 0) return true;
+        if ((nw != 1 && nw != 2 && nw != 4) || m < 1 || m > 4 || 32 * nw * m < n) {
+            why = std::string("invalid ") + fam + " line tile (warps 1, 2 or 4; 1..4 elements per thread; "
+                  "32*warps*elements >= line length)";
+            return false;
+        }
+        return true;
+    };
+    if (!tile_ok(p->tile_r_warps, p->tile_r_m, p->ni - 1, "radial")) return FVM_ERR_ARG;
+    if (!tile_ok(p->tile_t_warps, p->tile_t_m, p->nj - 1, "circumferential")) return FVM_ERR_ARG;
     return FVM_OK;
 }
 

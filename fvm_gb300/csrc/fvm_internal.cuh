@@ -56,6 +56,16 @@ struct PCtl {
     double pad3;
 };
 
+// Batch-wide control block of a batched launch (device memory).
+struct BatchCtl {
+    int remaining;      // cases whose Poisson iteration of this step is still running
+    int ncases;
+    int step;           // steps recorded in the current batch call
+    int bodies;         // Poisson loop bodies run in this step
+    int max_bodies;     // bound on bodies per step (every case reaches its cap before)
+    int overrun;        // set if the bound ended the loop
+};
+
 // Everything a kernel needs, passed by value.
 struct Dev {
     int NI, NJ, NI1, n;
@@ -66,6 +76,11 @@ struct Dev {
     int dd_pos;         // 1: cell (i,j) takes the cross term of cell (i-1,j-1) in DIF / ITER_P
     int refine_sweeps;  // MIXED: FP32 sweeps per FP64 refinement
     int adi_refine;     // MIXED: defect-correction passes of a predictor line
+    int nblk_res;       // blocks of this case in the residual kernels
+    int case_id;        // position in a batch
+    BatchCtl *bctl;     // batch control (nullptr in a single-context launch)
+    fvm_coeffs *bhist;  // batch: coefficient records [step * ncases + case]
+    double *btime;      // batch: the case's simulated time, advanced on the device
     // geometry
     double *XG, *YG, *X, *Y, *XIX, *XIY, *ETX, *ETY, *DJAC, *Q11, *Q12, *Q22;
     double *DE, *DW, *DN, *DS, *THETA, *AREA;
@@ -97,6 +112,14 @@ struct Dev {
     Coef cP, cUX, cUY, cTX, cTY;
     LineSys sP, sUX, sUY, sTX, sTY;
 };
+
+// Source of a kernel's Dev: one context (the Dev itself, passed by value) or a
+// batch (a table of Dev in device memory, one per case, case = blockIdx.z).
+struct DevTable {
+    const Dev *devs;
+};
+__device__ __forceinline__ const Dev &dev_of(const Dev &d) { return d; }
+__device__ __forceinline__ const Dev &dev_of(const DevTable &t) { return t.devs[blockIdx.z]; }
 
 }  // namespace fvm
 
@@ -155,7 +178,31 @@ struct fvm_ctx {
     } while (0)
 
 namespace fvm {
+// Where the launches of a step go: one context, or a batch of contexts advanced
+// together (grid z = case; x/y extents are the maxima over the cases, surplus
+// blocks of smaller cases return at once).  The cases of a batch share the line
+// tiles and the run options that shape the launch sequence.
+struct Tgt {
+    fvm_ctx *c = nullptr;        // error text and launch counters
+    cudaStream_t st = nullptr;   // stream the launches go to
+    const Dev *one = nullptr;    // single context: its device view (passed by value)
+    DevTable tab{nullptr};       // batch: device table of the cases' views
+    int nz = 1;                  // cases
+    int NI = 0, NJ = 0, n = 0, nblk_res = 0;   // launch extents
+    LineSys tr{}, tt{};          // tiles (NW, M) of the radial and circumferential line families
+    int mixed = 0, thermal = 1, iter_t_bug = 1, refine_sweeps = 1, res_every = 2;
+};
+
+template <class F>
+inline void with_src(const Tgt &t, F &&f)
+{
+    if (t.tab.devs) f(t.tab);
+    else f(*t.one);
+}
+
+Tgt tgt_of(fvm_ctx *c);
 int setup_allocate(fvm_ctx *c);
+int setup_factors(fvm_ctx *c);
 int setup_grid(fvm_ctx *c);
 int setup_init(fvm_ctx *c, const double *du, const double *dv);
 int run_begin_step(fvm_ctx *c);
@@ -171,14 +218,20 @@ int run_iter_t(fvm_ctx *c);
 int run_calccoef(fvm_ctx *c, fvm_coeffs *out);
 int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out);
 double *array_by_name(fvm_ctx *c, const char *name);
-// mixed precision (fvm_mixed.cu)
-int mixed_poisson_body(fvm_ctx *c, cudaGraphConditionalHandle cond, int has_cond);
-int mixed_sweep_pair(fvm_ctx *c, int apply);
 int run_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches);
-int mixed_predictor_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi,
-                           int colour, int refresh, const double *wallF, const double *farF);
-int mixed_predictor_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi,
-                          int colour, int ghosts, const double *wallF, const double *farF);
+// launch sequences shared by single contexts and batches (fvm_step.cu)
+int step_before_poisson(const Tgt &t);
+int poisson_bodies(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond, int groups);
+int step_after_poisson(const Tgt &t, double rtime, fvm_coeffs *dout);
+int sweep_pairs(const Tgt &t, int sweeps);
+int launch_batch_tick(const Tgt &t, BatchCtl *b);
+int theta_pairs(const Tgt &t, int field, int sweeps);
+int predictor_sweeps(const Tgt &t, int field);
+// mixed precision (fvm_mixed.cu)
+int mixed_poisson_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond);
+int mixed_sweep_pair(const Tgt &t, int apply);
+int mixed_predictor_radial(const Tgt &t, int field, int colour, int refresh);
+int mixed_predictor_theta(const Tgt &t, int field, int colour, int ghosts);
 }  // namespace fvm
 
 // ---------------------------------------------------------------------------------

@@ -21,12 +21,15 @@ namespace fvm {
 
 // FP64 residual of the current P, scaled-L1 norm, FP32 right-hand side of the
 // correction sweeps and zeroed correction.  The last block decides convergence.
-template <int HAS_COND>
-__global__ void __launch_bounds__(256) k_mres(Dev d, cudaGraphConditionalHandle cond)
+template <int HAS_COND, class S>
+__global__ void __launch_bounds__(256) k_mres(const __grid_constant__ S src, cudaGraphConditionalHandle cond)
 {
     __shared__ double sh[64];
     __shared__ bool last;
+    const Dev &d = dev_of(src);
+    if ((int)blockIdx.x >= d.nblk_res) return;   // beyond this case's blocks (batch)
     griddep_wait();
+    batch_body_guard<HAS_COND>(d, cond);
     if (d.pctl->done) return;
     const int it = d.pctl->niter;
     const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
@@ -52,7 +55,7 @@ __global__ void __launch_bounds__(256) k_mres(Dev d, cudaGraphConditionalHandle 
         if (it > 0 && !(resip > d.resimax && it < d.nswpp)) {
             d.pctl->done = 1;
             d.pctl->capped = (resip > d.resimax) ? 1 : 0;
-            if (HAS_COND) cudaGraphSetConditional(cond, 0);
+            poisson_finished<HAS_COND>(d, cond);
         } else {
             d.pctl->niter = it + d.refine_sweeps;
         }
@@ -62,12 +65,14 @@ __global__ void __launch_bounds__(256) k_mres(Dev d, cudaGraphConditionalHandle 
 // One zebra colour of the FP32 correction sweep on radial rows.  With apply != 0
 // (the last colour-1 sweep of an outer iteration) the warp of even row j also adds
 // the correction of rows j and j-1 to P in FP64 and refreshes their BCP ghosts.
-template <int M, int NW>
-__global__ void __launch_bounds__(128) k_pois32(Dev d, int colour, int apply, int check_done)
+template <int M, int NW, class S>
+__global__ void __launch_bounds__(128) k_pois32(const __grid_constant__ S src, int colour, int apply, int check_done)
 {
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ float sm[G][TG * M + M * NW + 1];
     __shared__ float xch[G][2 * NW];
+    const Dev &d = dev_of(src);
+    if ((int)blockIdx.x * G >= (d.NJ - 1) / 2) return;   // beyond this case's lines (batch)
     int gl, t, gib;
     group_of<NW>(gl, t, gib);
     const bool active = gl < (d.NJ - 1) / 2;
@@ -127,39 +132,43 @@ __global__ void __launch_bounds__(128) k_pois32(Dev d, int colour, int apply, in
 
 // One zebra sweep of the FP32 correction (both colours); apply != 0 also adds the
 // correction to P.  check_done is off when the pair is replayed for timing.
-static int sweep_pair(fvm_ctx *c, int apply, int check_done)
+static int sweep_pair(const Tgt &t, int apply, int check_done)
 {
-    Dev &d = c->d;
-    const int blocks = line_blocks((c->NJ - 1) / 2, d.sP.NW);
-    bool ok = dispatch_line(d.sP, [&](auto m, auto nw) {
-        auto k = k_pois32<decltype(m)::value, decltype(nw)::value>;
-        launch_pdl(k, dim3(blocks), dim3(128), c->stream, d, 0, 0, check_done);
-        launch_pdl(k, dim3(blocks), dim3(128), c->stream, d, 1, apply, check_done);
+    const int blocks = line_blocks((t.NJ - 1) / 2, t.tr.NW);
+    bool ok = dispatch_line(t.tr, [&](auto m, auto nw) {
+        with_src(t, [&](const auto &src) {
+            using S = std::decay_t<decltype(src)>;
+            auto k = k_pois32<decltype(m)::value, decltype(nw)::value, S>;
+            launch_pdl(k, dim3(blocks, 1, t.nz), dim3(128), t.st, src, 0, 0, check_done);
+            launch_pdl(k, dim3(blocks, 1, t.nz), dim3(128), t.st, src, 1, apply, check_done);
+        });
     });
     if (!ok) {
-        c->err = "line length above 512 cells is not supported";
+        t.c->err = "line length above 512 cells is not supported";
         return FVM_ERR_ARG;
     }
-    KCOUNT(c);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
+    KCOUNT(t.c);
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
     return FVM_OK;
 }
 
-int mixed_sweep_pair(fvm_ctx *c, int apply) { return sweep_pair(c, apply, 0); }
+int mixed_sweep_pair(const Tgt &t, int apply) { return sweep_pair(t, apply, 0); }
 
 // One outer iteration of the MIXED Poisson: FP64 residual (ends the device-side
 // loop when converged or capped), then refine_sweeps FP32 zebra sweeps, the last
 // of which adds the correction to P.
-int mixed_poisson_body(fvm_ctx *c, cudaGraphConditionalHandle cond, int has_cond)
+int mixed_poisson_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond)
 {
-    Dev &d = c->d;
-    if (has_cond) launch_pdl(k_mres<1>, dim3(c->nblk_res), dim3(256), c->stream, d, cond);
-    else launch_pdl(k_mres<0>, dim3(c->nblk_res), dim3(256), c->stream, d, cond);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
-    for (int s = 0; s < d.refine_sweeps; s++) {
-        int rc = sweep_pair(c, s == d.refine_sweeps - 1, 1);
+    with_src(t, [&](const auto &src) {
+        using S = std::decay_t<decltype(src)>;
+        if (has_cond) launch_pdl(k_mres<1, S>, dim3(t.nblk_res, 1, t.nz), dim3(256), t.st, src, cond);
+        else launch_pdl(k_mres<0, S>, dim3(t.nblk_res, 1, t.nz), dim3(256), t.st, src, cond);
+    });
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
+    for (int s = 0; s < t.refine_sweeps; s++) {
+        int rc = sweep_pair(t, s == t.refine_sweeps - 1, 1);
         if (rc) return rc;
     }
     return FVM_OK;
@@ -171,14 +180,20 @@ int mixed_poisson_body(fvm_ctx *c, cudaGraphConditionalHandle cond, int has_cond
 // Radial row j: -AW x(i-1) + AP x(i) - AE x(i+1) = C (AW(1)=0, AE(NI-1)=0 folded).
 // The line's FP64 values are staged in shared memory in natural order so that the
 // defect r = C - T x reads its neighbours there.
-template <int M, int NW>
-__global__ void __launch_bounds__(128) k_rad_dc(Dev d, LineSys s, Coef cf, const double *SU, double *phi, int colour,
-                                                int refresh, const double *wallF, const double *farF)
+template <int M, int NW, class S>
+__global__ void __launch_bounds__(128) k_rad_dc(const __grid_constant__ S src, int field, int colour, int refresh)
 {
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ double sx[G][TG * M + M * NW + 1];
     __shared__ float sm[G][TG * M + M * NW + 1];
     __shared__ float xch[G][2 * NW];
+    const Dev &d = dev_of(src);
+    if ((int)blockIdx.x * G >= (d.NJ - 1) / 2) return;   // beyond this case's lines (batch)
+    const PredLine L = pred_line(d, field, 0);
+    const LineSys &s = L.s;
+    const Coef &cf = L.cf;
+    const double *SU = L.SU, *wallF = L.wallF, *farF = L.farF;
+    double *phi = L.phi;
     int gl, t, gib;
     group_of<NW>(gl, t, gib);
     const bool active = gl < (d.NJ - 1) / 2;
@@ -231,14 +246,20 @@ __global__ void __launch_bounds__(128) k_rad_dc(Dev d, LineSys s, Coef cf, const
 }
 
 // Circumferential column i, cyclic: -AS x(j-1) + AP x(j) - AN x(j+1) = C.
-template <int M, int NW>
-__global__ void __launch_bounds__(128) k_theta_dc(Dev d, LineSys s, Coef cf, const double *SU, double *phi,
-                                                  int colour, int ghosts, const double *wallF, const double *farF)
+template <int M, int NW, class S>
+__global__ void __launch_bounds__(128) k_theta_dc(const __grid_constant__ S src, int field, int colour, int ghosts)
 {
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ double sx[G][TG * M + M * NW + 1];
     __shared__ float sm[G][TG * M + M * NW + 1];
     __shared__ float xch[G][2 * NW];
+    const Dev &d = dev_of(src);
+    if (2 * (int)blockIdx.x * G + 1 + colour > d.NI - 1) return;   // beyond this case's lines (batch)
+    const PredLine L = pred_line(d, field, 1);
+    const LineSys &s = L.s;
+    const Coef &cf = L.cf;
+    const double *SU = L.SU, *wallF = L.wallF, *farF = L.farF;
+    double *phi = L.phi;
     int gl, t, gib;
     group_of<NW>(gl, t, gib);
     const int i0 = 2 * gl + 1 + colour;
@@ -290,39 +311,41 @@ __global__ void __launch_bounds__(128) k_theta_dc(Dev d, LineSys s, Coef cf, con
     }
 }
 
-int mixed_predictor_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi, int colour,
-                           int refresh, const double *wallF, const double *farF)
+int mixed_predictor_radial(const Tgt &t, int field, int colour, int refresh)
 {
-    const Dev &d = c->d;
-    const int blocks = line_blocks((c->NJ - 1) / 2, s.NW);
-    bool ok = dispatch_line(s, [&](auto m, auto nw) {
-        k_rad_dc<decltype(m)::value, decltype(nw)::value>
-            <<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, refresh, wallF, farF);
+    const int blocks = line_blocks((t.NJ - 1) / 2, t.tr.NW);
+    bool ok = dispatch_line(t.tr, [&](auto m, auto nw) {
+        with_src(t, [&](const auto &src) {
+            using S = std::decay_t<decltype(src)>;
+            k_rad_dc<decltype(m)::value, decltype(nw)::value, S>
+                <<<dim3(blocks, 1, t.nz), 128, 0, t.st>>>(src, field, colour, refresh);
+        });
     });
     if (!ok) {
-        c->err = "line length above 512 cells is not supported";
+        t.c->err = "line length above 512 cells is not supported";
         return FVM_ERR_ARG;
     }
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
     return FVM_OK;
 }
 
-int mixed_predictor_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi, int colour,
-                          int ghosts, const double *wallF, const double *farF)
+int mixed_predictor_theta(const Tgt &t, int field, int colour, int ghosts)
 {
-    const Dev &d = c->d;
-    const int blocks = line_blocks((c->NI - 1 + 1 - colour) / 2, s.NW);
-    bool ok = dispatch_line(s, [&](auto m, auto nw) {
-        k_theta_dc<decltype(m)::value, decltype(nw)::value>
-            <<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, ghosts, wallF, farF);
+    const int blocks = line_blocks((t.NI - 1 + 1 - colour) / 2, t.tt.NW);
+    bool ok = dispatch_line(t.tt, [&](auto m, auto nw) {
+        with_src(t, [&](const auto &src) {
+            using S = std::decay_t<decltype(src)>;
+            k_theta_dc<decltype(m)::value, decltype(nw)::value, S>
+                <<<dim3(blocks, 1, t.nz), 128, 0, t.st>>>(src, field, colour, ghosts);
+        });
     });
     if (!ok) {
-        c->err = "line length above 512 cells is not supported";
+        t.c->err = "line length above 512 cells is not supported";
         return FVM_ERR_ARG;
     }
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
     return FVM_OK;
 }
 

@@ -188,20 +188,70 @@ __device__ __forceinline__ bool grid_sum2(const Dev &d, double &a, double &b, do
         d.partial[2 * blockIdx.x] = a;
         d.partial[2 * blockIdx.x + 1] = b;
         __threadfence();
-        unsigned t = atomicInc(&d.pctl->ticket, gridDim.x - 1);
-        last = (t == gridDim.x - 1);
+        const unsigned nb = (unsigned)d.nblk_res;
+        unsigned t = atomicInc(&d.pctl->ticket, nb - 1);
+        last = (t == nb - 1);
     }
     __syncthreads();
     if (!last) return false;
     __threadfence();
     a = 0.0;
     b = 0.0;
-    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    for (int k = threadIdx.x; k < d.nblk_res; k += blockDim.x) {
         a += ((volatile double *)d.partial)[2 * k];
         b += ((volatile double *)d.partial)[2 * k + 1];
     }
     block_sum2(a, b, sh);
     return true;
+}
+
+// A case's Poisson iteration has ended (converged or capped).  Inside a batch the
+// case leaves the count of running cases; the device-side loop ends with the last.
+// Once per loop body (case 0, first thread of the residual kernel): a batch's
+// device-side loop ends after max_bodies bodies whatever the cases report, so a
+// lost completion count cannot keep the GPU looping.
+template <int HAS_COND>
+__device__ __forceinline__ void batch_body_guard(const Dev &d, cudaGraphConditionalHandle cond)
+{
+    if (!d.bctl || d.case_id != 0 || blockIdx.x != 0 || threadIdx.x != 0) return;
+    const int b = d.bctl->bodies + 1;
+    d.bctl->bodies = b;
+    if (b > d.bctl->max_bodies) {
+        d.bctl->overrun = 1;
+        if (HAS_COND) cudaGraphSetConditional(cond, 0);
+    }
+}
+
+template <int HAS_COND>
+__device__ __forceinline__ void poisson_finished(const Dev &d, cudaGraphConditionalHandle cond)
+{
+    bool last = true;
+    if (d.bctl) last = atomicSub(&d.bctl->remaining, 1) == 1;
+    if (HAS_COND && last) cudaGraphSetConditional(cond, 0);
+}
+
+// Line system, coefficients, right-hand side, field and boundary values of one
+// predictor factor of a field (dir 0: radial lines of the first factor, 1:
+// circumferential lines of the second).
+struct PredLine {
+    LineSys s;
+    Coef cf;
+    const double *SU;
+    double *phi;
+    const double *wallF, *farF;
+};
+
+__device__ __forceinline__ PredLine pred_line(const Dev &d, int field, int dir)
+{
+    const bool tk = field == FVM_FIELD_T;
+    PredLine L;
+    L.s = dir == 0 ? (tk ? d.sTX : d.sUX) : (tk ? d.sTY : d.sUY);
+    L.cf = dir == 0 ? (tk ? d.cTX : d.cUX) : (tk ? d.cTY : d.cUY);
+    L.phi = field == FVM_FIELD_U ? d.U : (field == FVM_FIELD_V ? d.V : d.T);
+    L.SU = field == FVM_FIELD_U ? d.SU : (field == FVM_FIELD_V ? d.SUV : d.SUT);
+    L.wallF = field == FVM_FIELD_U ? d.UFW : (field == FVM_FIELD_V ? d.VFW : d.TFW);
+    L.farF = field == FVM_FIELD_U ? d.FFU : (field == FVM_FIELD_V ? d.FFV : d.FFT);
+    return L;
 }
 
 // Five-point Poisson residual (iter_p.f90:42-44) of P with the line neighbours

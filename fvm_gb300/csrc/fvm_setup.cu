@@ -26,14 +26,18 @@ struct Bump {
     }
 };
 
-void carve_sys(Bump &b, LineSys &s, int lines, int n, int cyclic)
+// Line tile of a family: warps per line group and elements per thread, either
+// given (both > 0, validated when the context is created) or derived from n.
+void carve_sys(Bump &b, LineSys &s, int lines, int n, int cyclic, int nw, int m)
 {
     s.lines = lines;
     s.n = n;
-    s.NW = group_warps(n);
-    s.M = (n + WARP * s.NW - 1) / (WARP * s.NW);
+    s.NW = nw > 0 ? nw : group_warps(n);
+    s.M = m > 0 ? m : (n + WARP * s.NW - 1) / (WARP * s.NW);
     s.cyclic = cyclic;
-    size_t cnt = size_t(lines) * WARP * s.NW * s.M;
+    // capacity for the largest tile (4 warps x 4 elements), so that the tile can
+    // be changed later without reallocation; the layout in use is dense
+    size_t cnt = size_t(lines) * WARP * 4 * 4;
     s.invD = b.take<double>(cnt);
     s.fa = b.take<double>(cnt);
     s.fb = b.take<double>(cnt);
@@ -94,11 +98,12 @@ void carve(Bump &b, fvm_ctx *c, int nblk)
     carve_coef(b, d.cTX, n, nj1);
     carve_coef(b, d.cTY, n, nj1);
     const int nr = c->NI - 1, nt = c->NJ - 1;
-    carve_sys(b, d.sP, nt, nr, 0);
-    carve_sys(b, d.sUX, nt, nr, 0);
-    carve_sys(b, d.sUY, nr, nt, 1);
-    carve_sys(b, d.sTX, nt, nr, 0);
-    carve_sys(b, d.sTY, nr, nt, 1);
+    const int rw = c->p.tile_r_warps, rm = c->p.tile_r_m, tw = c->p.tile_t_warps, tm = c->p.tile_t_m;
+    carve_sys(b, d.sP, nt, nr, 0, rw, rm);
+    carve_sys(b, d.sUX, nt, nr, 0, rw, rm);
+    carve_sys(b, d.sUY, nr, nt, 1, tw, tm);
+    carve_sys(b, d.sTX, nt, nr, 0, rw, rm);
+    carve_sys(b, d.sTY, nr, nt, 1, tw, tm);
 }
 
 }  // namespace
@@ -135,6 +140,7 @@ int setup_allocate(fvm_ctx *c)
     d.adi_refine = c->p.adi_refine < 1 ? 1 : c->p.adi_refine;
     const int interior = (c->NI - 1) * (c->NJ - 1);
     c->nblk_res = (interior + 256 * RES_CELLS - 1) / (256 * RES_CELLS);   // residual kernels
+    d.nblk_res = c->nblk_res;
     Bump probe{nullptr};
     carve(probe, c, c->nblk_res);
     c->slab_bytes = probe.off + 256;
@@ -439,6 +445,23 @@ static int build_line_sets(fvm_ctx *c)
     k_coef_af<<<grd, blk, 0, c->stream>>>(d, d.cTX, d.XIX, d.ETX, d.pe);
     k_coef_af<<<grd, blk, 0, c->stream>>>(d, d.cTY, d.XIY, d.ETY, d.pe);
     FVM_LAUNCH_CHECK(c);
+    return setup_factors(c);
+}
+
+// Line tiles from the parameters (0: automatic) and the factors of every line
+// family in the tile's layout.  Called at setup and again when the tile changes.
+int setup_factors(fvm_ctx *c)
+{
+    Dev &d = c->d;
+    auto tile = [](LineSys &s, int nw, int m) {
+        s.NW = nw > 0 ? nw : group_warps(s.n);
+        s.M = m > 0 ? m : (s.n + WARP * s.NW - 1) / (WARP * s.NW);
+    };
+    tile(d.sP, c->p.tile_r_warps, c->p.tile_r_m);
+    tile(d.sUX, c->p.tile_r_warps, c->p.tile_r_m);
+    tile(d.sTX, c->p.tile_r_warps, c->p.tile_r_m);
+    tile(d.sUY, c->p.tile_t_warps, c->p.tile_t_m);
+    tile(d.sTY, c->p.tile_t_warps, c->p.tile_t_m);
     struct { Coef *cf; LineSys *s; int circ; } sets[] = {
         {&d.cP, &d.sP, 0}, {&d.cUX, &d.sUX, 0}, {&d.cUY, &d.sUY, 1}, {&d.cTX, &d.sTX, 0}, {&d.cTY, &d.sTY, 1}};
     for (auto &st : sets) {

@@ -24,17 +24,22 @@ namespace fvm {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1; \
     if (i > d.NI - 1 || j > d.NJ - 1) return;
 
-__global__ void k_begin(Dev d)
-{   // Main.f90:52-54 (full arrays)
+template <class S>
+__global__ void k_begin(const __grid_constant__ S src)
+{   // Main.f90:49-54 (full arrays); a batch advances the case's time here
+    const Dev &d = dev_of(src);
     int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d.btime && k == 0) *d.btime = *d.btime + d.dt;
     if (k >= d.n) return;
     d.U_N[k] = d.U[k];
     d.V_N[k] = d.V[k];
     d.T_N[k] = d.T[k];
 }
 
-__global__ void k_farfield_step(Dev d)
+template <class S>
+__global__ void k_farfield_step(const __grid_constant__ S src)
 {
+    const Dev &d = dev_of(src);
     int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (j > d.NJ - 1) return;
     const int NI = d.NI;
@@ -55,8 +60,10 @@ __global__ void k_farfield_step(Dev d)
 
 // CONTRA_VEL (contra_vel.f90:9-21,125); with_poisson additionally forms the
 // Poisson source (1/dt)*div (iter_p.f90:27-29) and resets the iteration control.
-__global__ void k_contra_vel(Dev d, int with_poisson)
+template <class S>
+__global__ void k_contra_vel(const __grid_constant__ S src, int with_poisson)
 {
+    const Dev &d = dev_of(src);
     INTERIOR_IJ
     const double *J = d.DJAC;
     int c = IDX(i, j), e = IDX(i + 1, j), w = IDX(i - 1, j), nn = IDX(i, j + 1), s = IDX(i, j - 1);
@@ -76,6 +83,10 @@ __global__ void k_contra_vel(Dev d, int with_poisson)
             d.pctl->done = 0;
             d.pctl->capped = 0;
             d.pctl->resip = 0.0;
+            if (d.bctl && d.case_id == 0) {
+                d.bctl->remaining = d.bctl->ncases;
+                d.bctl->bodies = 0;
+            }
         }
     }
 }
@@ -108,8 +119,10 @@ __global__ void k_psource(Dev d)
 
 // Fused explicit phase of a step (Main.f90:61-74 plus the first-factor right-hand
 // sides of ITER_U/ITER_V/ITER_T, which depend only on step-n data).
-__global__ void k_explicit(Dev d, int thermal)
+template <class S>
+__global__ void k_explicit(const __grid_constant__ S src, int thermal)
 {
+    const Dev &d = dev_of(src);
     INTERIOR_IJ
     int c = IDX(i, j);
     d.NLX_NM1[c] = d.NLX[c];
@@ -141,12 +154,16 @@ __global__ void k_af_su1(Dev d, int field)
 }
 
 // Second-factor right-hand side (iter_u.f90:86-99, iter_T.f90:86-98) with the
-// BCU folding; cross term from xfield (V for ITER_T when the reference's V is kept).
-__global__ void k_af_su2(Dev d, int field, const double *xfield)
+// BCU folding; the cross term of ITER_T is built from V when v_cross is set (the
+// reference's iter_T.f90:89-95), else from the field itself.
+template <class S>
+__global__ void k_af_su2(const __grid_constant__ S src, int field, int v_cross)
 {
+    const Dev &d = dev_of(src);
     INTERIOR_IJ
     int c = IDX(i, j);
     FieldRefs f = field_refs(d, field);
+    const double *xfield = (field == FVM_FIELD_T && v_cross) ? d.V : f.phi;
     const bool tk = field == FVM_FIELD_T;
     const double *JDT = tk ? d.PJDT : d.RJDT;
     double s = JDT[c] * f.phi[c] + cross_at(d, d.JYE, xfield, i, j);
@@ -159,8 +176,10 @@ __global__ void k_af_su2(Dev d, int field, const double *xfield)
 // u^ = u* -/+ dt S/J on the interior (Main.f90:80-84, 99-103) with the BCU/BCV ghost
 // refresh of the updated cells.  with_psource recomputes S from P first and derives
 // the P ghosts of BCP (bcp.f90:19-30,36-42) from the interior as well.
-__global__ void k_grad(Dev d, double sign, int with_psource)
+template <class S>
+__global__ void k_grad(const __grid_constant__ S src, double sign, int with_psource)
 {
+    const Dev &d = dev_of(src);
     INTERIOR_IJ
     int c = IDX(i, j);
     double su, sv;
@@ -210,8 +229,10 @@ __global__ void k_grad(Dev d, double sign, int with_psource)
 }
 
 // BCP ghost refresh from the interior (bcp.f90:19-30, 36-42) over every ghost cell.
-__global__ void k_bcp_ghosts(Dev d)
+template <class S>
+__global__ void k_bcp_ghosts(const __grid_constant__ S src)
 {
+    const Dev &d = dev_of(src);
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int NI = d.NI, NJ = d.NJ;
     double *P = d.P;
@@ -239,13 +260,19 @@ __global__ void k_bcp_ghosts(Dev d)
 // with the neighbour rows read through periodic wrap (iter_u.f90:52-64).
 // Colour 0 first refreshes the ghosts of its own row and of the next (even) row
 // from the pre-sweep values (the BCU call at iter_u.f90:48).
-template <int M, int NW, int BCK>
-__global__ void __launch_bounds__(128) k_radial(Dev d, LineSys s, Coef cf, const double *SU, double *phi, int colour,
-                                                int refresh, const double *wallF, const double *farF)
+template <int M, int NW, int BCK, class S>
+__global__ void __launch_bounds__(128) k_radial(const __grid_constant__ S src, int field, int colour, int refresh)
 {
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ double sm[G][TG * M + M * NW + 1];
     __shared__ double xch[G][2 * NW];
+    const Dev &d = dev_of(src);
+    if ((int)blockIdx.x * G >= (d.NJ - 1) / 2) return;   // beyond this case's lines (batch)
+    const PredLine L = pred_line(d, field, 0);
+    const LineSys &s = L.s;
+    const Coef &cf = L.cf;
+    const double *SU = L.SU, *wallF = L.wallF, *farF = L.farF;
+    double *phi = L.phi;
     int gl, t, gib;
     group_of<NW>(gl, t, gib);
     const bool active = gl < (d.NJ - 1) / 2;
@@ -282,13 +309,19 @@ __global__ void __launch_bounds__(128) k_radial(Dev d, LineSys s, Coef cf, const
 //   -AS x(j-1) + AP x(j) - AN x(j+1) = AE phi(i+1,j) + AW phi(i-1,j) + SU
 // (iter_u.f90:104-119 with the periodic coupling made implicit).  ghosts != 0 also
 // writes the BCT/BCU ghost cells derived from the new values.
-template <int M, int NW>
-__global__ void __launch_bounds__(128) k_theta(Dev d, LineSys s, Coef cf, const double *SU, double *phi, int colour,
-                                               int ghosts, const double *wallF, const double *farF)
+template <int M, int NW, class S>
+__global__ void __launch_bounds__(128) k_theta(const __grid_constant__ S src, int field, int colour, int ghosts)
 {
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ double sm[G][TG * M + M * NW + 1];
     __shared__ double xch[G][2 * NW];
+    const Dev &d = dev_of(src);
+    if (2 * (int)blockIdx.x * G + 1 + colour > d.NI - 1) return;   // beyond this case's lines (batch)
+    const PredLine L = pred_line(d, field, 1);
+    const LineSys &s = L.s;
+    const Coef &cf = L.cf;
+    const double *SU = L.SU, *wallF = L.wallF, *farF = L.farF;
+    double *phi = L.phi;
     int gl, t, gib;
     group_of<NW>(gl, t, gib);
     const int i0 = 2 * gl + 1 + colour;
@@ -329,12 +362,16 @@ __global__ void __launch_bounds__(128) k_theta(Dev d, LineSys s, Coef cf, const 
 // rows from Pin, colour 1 (even rows) from Pout, exactly the in-place zebra order,
 // while DD of both colours still sees P^(n-1) as the reference's lagged term does.
 // ---------------------------------------------------------------------------------
-template <int M, int NW>
-__global__ void __launch_bounds__(128) k_pois64(Dev d, const double *Pin, double *Pout, int colour, int check_done)
+template <int M, int NW, class S>
+__global__ void __launch_bounds__(128) k_pois64(const __grid_constant__ S src, int parity, int colour, int check_done)
 {
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ double sm[G][TG * M + M * NW + 1];
     __shared__ double xch[G][2 * NW];
+    const Dev &d = dev_of(src);
+    if ((int)blockIdx.x * G >= (d.NJ - 1) / 2) return;   // beyond this case's lines (batch)
+    const double *Pin = parity ? d.P2 : d.P;
+    double *Pout = parity ? d.P : d.P2;
     int gl, t, gib;
     group_of<NW>(gl, t, gib);
     const bool active = gl < (d.NJ - 1) / 2;
@@ -389,12 +426,15 @@ __global__ void __launch_bounds__(128) k_pois64(Dev d, const double *Pin, double
 // last sweep is rebuilt from P^(n-1) (with its stored ghosts).  The last block
 // publishes the count and decides convergence (iter_p.f90:50-51); inside the
 // device-side loop it also ends the loop (cond != 0).
-template <int HAS_COND>
-__global__ void __launch_bounds__(256) k_pres64(Dev d, cudaGraphConditionalHandle cond)
+template <int HAS_COND, class S>
+__global__ void __launch_bounds__(256) k_pres64(const __grid_constant__ S src, cudaGraphConditionalHandle cond)
 {
     __shared__ double sh[64];
     __shared__ bool last;
+    const Dev &d = dev_of(src);
+    if ((int)blockIdx.x >= d.nblk_res) return;   // beyond this case's blocks (batch)
     griddep_wait();
+    batch_body_guard<HAS_COND>(d, cond);
     if (d.pctl->done) return;
     const int it = d.pctl->niter + d.res_every;
     const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
@@ -419,7 +459,7 @@ __global__ void __launch_bounds__(256) k_pres64(Dev d, cudaGraphConditionalHandl
         if (!(resip > d.resimax && it < d.nswpp)) {
             d.pctl->done = 1;
             d.pctl->capped = (resip > d.resimax) ? 1 : 0;
-            if (HAS_COND) cudaGraphSetConditional(cond, 0);
+            poisson_finished<HAS_COND>(d, cond);
         }
     }
 }
@@ -428,8 +468,10 @@ __global__ void __launch_bounds__(256) k_pres64(Dev d, cudaGraphConditionalHandl
 // CALCCOEF (calccoef.f90:9-120): per-j wall contributions, CFL maximum, then a
 // single-thread fixed-order sum (the reference's J order).
 // ---------------------------------------------------------------------------------
-__global__ void k_calc_rows(Dev d)
+template <class S>
+__global__ void k_calc_rows(const __grid_constant__ S src)
 {
+    const Dev &d = dev_of(src);
     int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (j > d.NJ - 1) return;
     const int c = IDX(1, j);
@@ -464,16 +506,24 @@ __global__ void k_calc_rows(Dev d)
     row[4] = dtdn * ar;
 }
 
-__global__ void k_cfl(Dev d)
+template <class S>
+__global__ void k_cfl(const __grid_constant__ S src)
 {
+    const Dev &d = dev_of(src);
     INTERIOR_IJ
     int c = IDX(i, j);
     double l = d.dt * (fabs(d.XIX[c] * d.U[c] + d.XIY[c] * d.V[c]) + fabs(d.ETX[c] * d.U[c] + d.ETY[c] * d.V[c]));
     atomicMax(d.cflbits, (unsigned long long)__double_as_longlong(l));
 }
 
-__global__ void k_calc_final(Dev d, double rtime, fvm_coeffs *out)
+template <class S>
+__global__ void k_calc_final(const __grid_constant__ S src, double rtime, fvm_coeffs *out)
 {
+    const Dev &d = dev_of(src);
+    if (d.bctl) {   // batch: the case's device time, one record per step and case
+        rtime = *d.btime;
+        out = d.bhist + (size_t)d.bctl->step * d.bctl->ncases + d.case_id;
+    }
     double pd = 0.0, pl = 0.0, td = 0.0, tl = 0.0, nu = 0.0;
     for (int j = 1; j <= d.NJ - 1; j++) {
         const double *row = d.coefrow + 8 * j;
@@ -500,49 +550,40 @@ __global__ void k_calc_final(Dev d, double rtime, fvm_coeffs *out)
     *d.cflbits = 0ull;
 }
 
+// Batch bookkeeping after a step's CALCCOEF: the next step's records follow.
+__global__ void k_batch_tick(BatchCtl *b)
+{
+    b->step = b->step + 1;
+}
+
 // ---------------------------------------------------------------------------------
-// Host launchers
+// Host launchers.  Every launch goes to a target: one context (Dev by value) or a
+// batch (Dev table, grid z = case).
 // ---------------------------------------------------------------------------------
+Tgt tgt_of(fvm_ctx *c)
+{
+    Tgt t;
+    t.c = c;
+    t.st = c->stream;
+    t.one = &c->d;
+    t.nz = 1;
+    t.NI = c->NI;
+    t.NJ = c->NJ;
+    t.n = c->n;
+    t.nblk_res = c->nblk_res;
+    t.tr = c->d.sP;
+    t.tt = c->d.sUY;
+    t.mixed = c->p.precision == FVM_MIXED;
+    t.thermal = c->p.thermal;
+    t.iter_t_bug = c->p.iter_t_bug;
+    t.refine_sweeps = c->d.refine_sweeps;
+    t.res_every = c->d.res_every;
+    return t;
+}
+
 namespace {
 
-inline dim3 interior_grid(const fvm_ctx *c) { return dim3((c->NI - 1 + 127) / 128, c->NJ - 1); }
-
-template <int BCK>
-int launch_radial(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi, int colour,
-                  int refresh, const double *wallF, const double *farF, int /*unused*/)
-{
-    const Dev &d = c->d;
-    const int blocks = line_blocks((c->NJ - 1) / 2, s.NW);
-    bool ok = dispatch_line(s, [&](auto m, auto nw) {
-        k_radial<decltype(m)::value, decltype(nw)::value, BCK>
-            <<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, refresh, wallF, farF);
-    });
-    if (!ok) {
-        c->err = "line length above 512 cells is not supported";
-        return FVM_ERR_ARG;
-    }
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
-    return FVM_OK;
-}
-
-int launch_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU, double *phi, int colour,
-                 int ghosts, const double *wallF, const double *farF)
-{
-    const Dev &d = c->d;
-    const int blocks = line_blocks((c->NI - 1 + 1 - colour) / 2, s.NW);
-    bool ok = dispatch_line(s, [&](auto m, auto nw) {
-        k_theta<decltype(m)::value, decltype(nw)::value>
-            <<<blocks, 128, 0, c->stream>>>(d, s, cf, SU, phi, colour, ghosts, wallF, farF);
-    });
-    if (!ok) {
-        c->err = "line length above 512 cells is not supported";
-        return FVM_ERR_ARG;
-    }
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
-    return FVM_OK;
-}
+inline dim3 interior_grid(const Tgt &t) { return dim3((t.NI - 1 + 127) / 128, t.NJ - 1, t.nz); }
 
 #define RC(x)                 \
     do {                      \
@@ -550,63 +591,200 @@ int launch_theta(fvm_ctx *c, const LineSys &s, const Coef &cf, const double *SU,
         if (rc_) return rc_;  \
     } while (0)
 
-// The predictor of one field after its first-factor SU is in place.
-int predictor_sweeps(fvm_ctx *c, int field)
+// Launch kernel template `kern` (instantiated for the target's Dev source) and
+// count / check it.
+#define LAUNCH_S(t, kern, grid, block, ...)                                   \
+    do {                                                                      \
+        with_src((t), [&](const auto &src_) {                                 \
+            using S_ = std::decay_t<decltype(src_)>;                          \
+            kern<S_><<<(grid), (block), 0, (t).st>>>(src_, ##__VA_ARGS__);    \
+        });                                                                   \
+        KCOUNT((t).c);                                                        \
+        FVM_LAUNCH_CHECK((t).c);                                              \
+    } while (0)
+
+int line_error(fvm_ctx *c)
 {
-    Dev &d = c->d;
-    const bool tk = field == FVM_FIELD_T;
-    const LineSys &sx = tk ? d.sTX : d.sUX;
-    const LineSys &sy = tk ? d.sTY : d.sUY;
-    const Coef &cx = tk ? d.cTX : d.cUX;
-    const Coef &cy = tk ? d.cTY : d.cUY;
-    double *phi = field == FVM_FIELD_U ? d.U : (field == FVM_FIELD_V ? d.V : d.T);
-    double *su = field == FVM_FIELD_U ? d.SU : (field == FVM_FIELD_V ? d.SUV : d.SUT);
-    const double *wf = field == FVM_FIELD_U ? d.UFW : (field == FVM_FIELD_V ? d.VFW : d.TFW);
-    const double *farF = field == FVM_FIELD_U ? d.FFU : (field == FVM_FIELD_V ? d.FFV : d.FFT);
-    const bool mixed = c->p.precision == FVM_MIXED;
-    // sweep 1 (radial lines), ghosts refreshed from the pre-sweep field (BCU)
-    for (int colour = 0; colour < 2; colour++) {
-        if (mixed) RC(mixed_predictor_radial(c, sx, cx, su, phi, colour, colour == 0, wf, farF));
-        else RC(launch_radial<BCK_DIRICHLET>(c, sx, cx, su, phi, colour, colour == 0, wf, farF, 0));
+    c->err = "line length above 512 cells is not supported";
+    return FVM_ERR_ARG;
+}
+
+int launch_radial(const Tgt &t, int field, int colour, int refresh)
+{
+    const int blocks = line_blocks((t.NJ - 1) / 2, t.tr.NW);
+    bool ok = dispatch_line(t.tr, [&](auto m, auto nw) {
+        with_src(t, [&](const auto &src) {
+            using S = std::decay_t<decltype(src)>;
+            k_radial<decltype(m)::value, decltype(nw)::value, BCK_DIRICHLET, S>
+                <<<dim3(blocks, 1, t.nz), 128, 0, t.st>>>(src, field, colour, refresh);
+        });
+    });
+    if (!ok) return line_error(t.c);
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
+    return FVM_OK;
+}
+
+int launch_theta(const Tgt &t, int field, int colour, int ghosts)
+{
+    const int blocks = line_blocks((t.NI - 1 + 1 - colour) / 2, t.tt.NW);
+    bool ok = dispatch_line(t.tt, [&](auto m, auto nw) {
+        with_src(t, [&](const auto &src) {
+            using S = std::decay_t<decltype(src)>;
+            k_theta<decltype(m)::value, decltype(nw)::value, S>
+                <<<dim3(blocks, 1, t.nz), 128, 0, t.st>>>(src, field, colour, ghosts);
+        });
+    });
+    if (!ok) return line_error(t.c);
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
+    return FVM_OK;
+}
+
+int launch_pois64(const Tgt &t, int parity, int colour, int check_done)
+{
+    const int blocks = line_blocks((t.NJ - 1) / 2, t.tr.NW);
+    bool ok = dispatch_line(t.tr, [&](auto m, auto nw) {
+        with_src(t, [&](const auto &src) {
+            using S = std::decay_t<decltype(src)>;
+            launch_pdl(k_pois64<decltype(m)::value, decltype(nw)::value, S>, dim3(blocks, 1, t.nz), dim3(128), t.st,
+                       src, parity, colour, check_done);
+        });
+    });
+    if (!ok) return line_error(t.c);
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
+    return FVM_OK;
+}
+
+// One residual interval of the FP64 iteration: res_every sweeps alternating
+// P -> P2 -> P, then the residual (which ends the device-side loop when done).
+int poisson64_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond)
+{
+    for (int it = 0; it < t.res_every; it++) {
+        RC(launch_pois64(t, it & 1, 0, 1));
+        RC(launch_pois64(t, it & 1, 1, 1));
     }
-    // second factor right-hand side from the first-sweep field
-    const double *xf = (tk && c->p.iter_t_bug) ? d.V : phi;
-    k_af_su2<<<interior_grid(c), 128, 0, c->stream>>>(d, field, xf);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
-    for (int colour = 0; colour < 2; colour++) {
-        if (mixed) RC(mixed_predictor_theta(c, sy, cy, su, phi, colour, tk ? 1 : 0, wf, farF));
-        else RC(launch_theta(c, sy, cy, su, phi, colour, tk ? 1 : 0, wf, farF));
-    }
+    with_src(t, [&](const auto &src) {
+        using S = std::decay_t<decltype(src)>;
+        if (has_cond) launch_pdl(k_pres64<1, S>, dim3(t.nblk_res, 1, t.nz), dim3(256), t.st, src, cond);
+        else launch_pdl(k_pres64<0, S>, dim3(t.nblk_res, 1, t.nz), dim3(256), t.st, src, cond);
+    });
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
     return FVM_OK;
 }
 
 }  // namespace
 
+// The predictor of one field after its first-factor SU is in place.
+int predictor_sweeps(const Tgt &t, int field)
+{
+    const bool tk = field == FVM_FIELD_T;
+    // sweep 1 (radial lines), ghosts refreshed from the pre-sweep field (BCU)
+    for (int colour = 0; colour < 2; colour++) {
+        if (t.mixed) RC(mixed_predictor_radial(t, field, colour, colour == 0));
+        else RC(launch_radial(t, field, colour, colour == 0));
+    }
+    // second factor right-hand side from the first-sweep field
+    LAUNCH_S(t, k_af_su2, interior_grid(t), 128, field, (tk && t.iter_t_bug) ? 1 : 0);
+    for (int colour = 0; colour < 2; colour++) {
+        if (t.mixed) RC(mixed_predictor_theta(t, field, colour, tk ? 1 : 0));
+        else RC(launch_theta(t, field, colour, tk ? 1 : 0));
+    }
+    return FVM_OK;
+}
+
+// Main.f90:48-93 up to the Poisson loop: step start, far-field values, fluxes,
+// explicit terms, the U and V predictors, the gradient removal and the Poisson
+// source.
+int step_before_poisson(const Tgt &t)
+{
+    LAUNCH_S(t, k_begin, dim3((t.n + 255) / 256, 1, t.nz), 256);
+    LAUNCH_S(t, k_farfield_step, dim3((t.NJ + 127) / 128, 1, t.nz), 128);
+    LAUNCH_S(t, k_contra_vel, interior_grid(t), 128, 0);
+    LAUNCH_S(t, k_explicit, interior_grid(t), 128, t.thermal);
+    RC(predictor_sweeps(t, FVM_FIELD_U));
+    RC(predictor_sweeps(t, FVM_FIELD_V));
+    LAUNCH_S(t, k_grad, interior_grid(t), 128, -1.0, 0);
+    LAUNCH_S(t, k_contra_vel, interior_grid(t), 128, 1);
+    return FVM_OK;
+}
+
+// `groups` residual intervals of the Poisson iteration.
+int poisson_bodies(const Tgt &t, cudaGraphConditionalHandle h, int has_cond, int groups)
+{
+    for (int g = 0; g < groups; g++) RC(t.mixed ? mixed_poisson_body(t, h, has_cond) : poisson64_body(t, h, has_cond));
+    return FVM_OK;
+}
+
+// Main.f90:93-114 after the Poisson loop: BCP ghosts, correction, ITER_T and the
+// CALCCOEF kernels (a single context's record goes to dout; a batch appends one
+// record per case to its history).
+int step_after_poisson(const Tgt &t, double rtime, fvm_coeffs *dout)
+{
+    LAUNCH_S(t, k_bcp_ghosts, dim3((t.NI + t.NJ + 127) / 128, 1, t.nz), 128);
+    LAUNCH_S(t, k_grad, interior_grid(t), 128, +1.0, 1);
+    if (t.thermal) RC(predictor_sweeps(t, FVM_FIELD_T));
+    LAUNCH_S(t, k_calc_rows, dim3((t.NJ + 127) / 128, 1, t.nz), 128);
+    LAUNCH_S(t, k_cfl, interior_grid(t), 128);
+    LAUNCH_S(t, k_calc_final, dim3(1, 1, t.nz), 1, rtime, dout);
+    return FVM_OK;
+}
+
+// `sweeps` zebra sweeps that touch only scratch (FP64: P -> P2 both colours;
+// MIXED: the FP32 correction without applying it), for timing.
+int sweep_pairs(const Tgt &t, int sweeps)
+{
+    for (int s = 0; s < sweeps; s++) {
+        if (t.mixed) RC(mixed_sweep_pair(t, 0));
+        else {
+            RC(launch_pois64(t, 0, 0, 0));
+            RC(launch_pois64(t, 0, 1, 0));
+        }
+    }
+    return FVM_OK;
+}
+
+// `sweeps` circumferential predictor sweeps of a field (both colours), for timing.
+int theta_pairs(const Tgt &t, int field, int sweeps)
+{
+    for (int s = 0; s < sweeps; s++)
+        for (int colour = 0; colour < 2; colour++) {
+            if (t.mixed) RC(mixed_predictor_theta(t, field, colour, 0));
+            else RC(launch_theta(t, field, colour, 0));
+        }
+    return FVM_OK;
+}
+
+int launch_batch_tick(const Tgt &t, BatchCtl *b)
+{
+    k_batch_tick<<<1, 1, 0, t.st>>>(b);
+    KCOUNT(t.c);
+    FVM_LAUNCH_CHECK(t.c);
+    return FVM_OK;
+}
+
 int run_begin_step(fvm_ctx *c)
 {
-    Dev &d = c->d;
     c->rtime = c->rtime + c->p.dt;
     c->niter_time += 1;
-    k_begin<<<(c->n + 255) / 256, 256, 0, c->stream>>>(d);
-    KCOUNT(c);
-    k_farfield_step<<<(c->NJ + 127) / 128, 128, 0, c->stream>>>(d);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
+    Tgt t = tgt_of(c);
+    LAUNCH_S(t, k_begin, dim3((t.n + 255) / 256, 1, 1), 256);
+    LAUNCH_S(t, k_farfield_step, dim3((t.NJ + 127) / 128, 1, 1), 128);
     return FVM_OK;
 }
 
 int run_contra_vel(fvm_ctx *c)
 {
-    k_contra_vel<<<interior_grid(c), 128, 0, c->stream>>>(c->d, 0);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
+    Tgt t = tgt_of(c);
+    LAUNCH_S(t, k_contra_vel, interior_grid(t), 128, 0);
     return FVM_OK;
 }
 
 int run_nl(fvm_ctx *c, int field)
 {
-    k_nl<<<interior_grid(c), 128, 0, c->stream>>>(c->d, field);
+    k_nl<<<interior_grid(tgt_of(c)), 128, 0, c->stream>>>(c->d, field);
     KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
@@ -614,7 +792,7 @@ int run_nl(fvm_ctx *c, int field)
 
 int run_dif(fvm_ctx *c, int field)
 {
-    k_dif<<<interior_grid(c), 128, 0, c->stream>>>(c->d, field);
+    k_dif<<<interior_grid(tgt_of(c)), 128, 0, c->stream>>>(c->d, field);
     KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
@@ -622,7 +800,7 @@ int run_dif(fvm_ctx *c, int field)
 
 int run_p_source(fvm_ctx *c)
 {
-    k_psource<<<interior_grid(c), 128, 0, c->stream>>>(c->d);
+    k_psource<<<interior_grid(tgt_of(c)), 128, 0, c->stream>>>(c->d);
     KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
     return FVM_OK;
@@ -630,72 +808,32 @@ int run_p_source(fvm_ctx *c)
 
 int run_iter_u(fvm_ctx *c, int field)
 {
-    k_af_su1<<<interior_grid(c), 128, 0, c->stream>>>(c->d, field);
+    k_af_su1<<<interior_grid(tgt_of(c)), 128, 0, c->stream>>>(c->d, field);
     KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
-    return predictor_sweeps(c, field);
+    return predictor_sweeps(tgt_of(c), field);
 }
 
 int run_remove_grad(fvm_ctx *c)
 {
-    k_grad<<<interior_grid(c), 128, 0, c->stream>>>(c->d, -1.0, 0);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
+    Tgt t = tgt_of(c);
+    LAUNCH_S(t, k_grad, interior_grid(t), 128, -1.0, 0);
     return FVM_OK;
 }
 
-int launch_pois64(fvm_ctx *c, const double *Pin, double *Pout, int colour, int check_done)
-{
-    const Dev &d = c->d;
-    const int blocks = line_blocks((c->NJ - 1) / 2, d.sP.NW);
-    bool ok = dispatch_line(d.sP, [&](auto m, auto nw) {
-        launch_pdl(k_pois64<decltype(m)::value, decltype(nw)::value>, dim3(blocks), dim3(128), c->stream, d, Pin,
-                   Pout, colour, check_done);
-    });
-    if (!ok) {
-        c->err = "line length above 512 cells is not supported";
-        return FVM_ERR_ARG;
-    }
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
-    return FVM_OK;
-}
+namespace {
 
-// One residual interval of the FP64 iteration: res_every sweeps alternating
-// P -> P2 -> P, then the residual (which ends the device-side loop when done).
-static int poisson64_body(fvm_ctx *c, cudaGraphConditionalHandle cond, int has_cond)
-{
-    Dev &d = c->d;
-    for (int it = 0; it < d.res_every; it++) {
-        const double *in = (it & 1) ? d.P2 : d.P;
-        double *out = (it & 1) ? d.P : d.P2;
-        RC(launch_pois64(c, in, out, 0, 1));
-        RC(launch_pois64(c, in, out, 1, 1));
-    }
-    if (has_cond) launch_pdl(k_pres64<1>, dim3(c->nblk_res), dim3(256), c->stream, d, cond);
-    else launch_pdl(k_pres64<0>, dim3(c->nblk_res), dim3(256), c->stream, d, cond);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
-    return FVM_OK;
-}
-
-// The whole Poisson iteration as one graph.  Device loop (default): a
+// The whole Poisson iteration of a context as one graph.  Device loop: a
 // while-conditional node whose body holds `groups` residual intervals; the residual
 // kernel clears the condition on convergence or at the sweep cap, so the loop ends
-// on the device without host synchronisation.  Host loop: the same body as a plain
-// graph, replayed by the host until the control block reports completion.
-static int body_groups(fvm_ctx *c, cudaGraphConditionalHandle h, int has_cond, int groups)
-{
-    const bool mixed = c->p.precision == FVM_MIXED;
-    for (int g = 0; g < groups; g++) RC(mixed ? mixed_poisson_body(c, h, has_cond) : poisson64_body(c, h, has_cond));
-    return FVM_OK;
-}
-
-static int poisson_graph(fvm_ctx *c)
+// on the device without host synchronisation.  Host loop (default): the same body
+// as a plain graph, replayed by the host until the control block reports
+// completion (profilers can then see each kernel).
+int poisson_graph(fvm_ctx *c)
 {
     if (c->pgraph) return FVM_OK;
-    const bool mixed = c->p.precision == FVM_MIXED;
-    const int per = mixed ? c->d.refine_sweeps : c->d.res_every;
+    Tgt t = tgt_of(c);
+    const int per = t.mixed ? t.refine_sweeps : t.res_every;
     int groups = c->p.poisson_groups > 0 ? c->p.poisson_groups : (32 + per - 1) / per;
     cudaGraph_t g = nullptr;
     cudaError_t e;
@@ -703,7 +841,7 @@ static int poisson_graph(fvm_ctx *c)
     if (c->p.poisson_host_loop) {
         FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         c->capturing = true;
-        int rc = body_groups(c, 0, 0, groups);
+        int rc = poisson_bodies(t, 0, 0, groups);
         c->capturing = false;
         e = cudaStreamEndCapture(c->stream, &g);
         if (rc || e != cudaSuccess) {
@@ -735,7 +873,7 @@ static int poisson_graph(fvm_ctx *c)
             return FVM_ERR_CUDA;
         }
         c->capturing = true;
-        int rc = body_groups(c, h, 1, groups);
+        int rc = poisson_bodies(t, h, 1, groups);
         c->capturing = false;
         cudaGraph_t body_out = body;
         e = cudaStreamEndCapture(c->stream, &body_out);
@@ -757,7 +895,7 @@ static int poisson_graph(fvm_ctx *c)
 
 // Kernel launches of a finished Poisson loop (for the launch counter): whole
 // bodies are launched, their kernels returning early once converged.
-static long long poisson_loop_kernels(fvm_ctx *c, int niter)
+long long poisson_loop_kernels(fvm_ctx *c, int niter)
 {
     const int per = c->pgraph_batch;
     const bool mixed = c->p.precision == FVM_MIXED;
@@ -766,56 +904,40 @@ static long long poisson_loop_kernels(fvm_ctx *c, int niter)
     return bodies * c->pgraph_kernels;
 }
 
-// Poisson phase of a step; with the device loop there is no host synchronisation
-// and the statistics stay on the device (CALCCOEF copies them with the
-// coefficients).
-static int iter_p_async(fvm_ctx *c)
+// The Poisson loop of a context after its source term is in place; with the
+// device loop there is no host synchronisation and the statistics stay on the
+// device (CALCCOEF copies them with the coefficients).
+int poisson_loop(fvm_ctx *c)
 {
     Dev &d = c->d;
-    k_contra_vel<<<interior_grid(c), 128, 0, c->stream>>>(d, 1);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
     RC(poisson_graph(c));
     if (!c->p.poisson_host_loop) {
         FVM_CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
-    } else {
-        const long max_launches = (long)d.nswpp / c->pgraph_batch + 2;
-        for (long launch = 0;; launch++) {
-            if (launch >= max_launches) {
-                c->err = "Poisson iteration did not report completion within the sweep cap";
-                return FVM_ERR_TIMEOUT;
-            }
-            FVM_CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
-            FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
-            FVM_CUDA(c, cudaStreamSynchronize(c->stream));
-            if (c->h_pctl->done) break;
-        }
+        return FVM_OK;
     }
-    k_bcp_ghosts<<<(c->NI + c->NJ + 127) / 128, 128, 0, c->stream>>>(d);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
+    const long max_launches = (long)d.nswpp / c->pgraph_batch + 2;
+    for (long launch = 0;; launch++) {
+        if (launch >= max_launches) {
+            c->err = "Poisson iteration did not report completion within the sweep cap";
+            return FVM_ERR_TIMEOUT;
+        }
+        FVM_CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
+        FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
+        FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (c->h_pctl->done) break;
+    }
     return FVM_OK;
 }
 
-// Sweep kernels alone, for timing: `sweeps` zebra sweeps that touch only scratch
-// (FP64: P -> P2 both colours; MIXED: the FP32 correction without applying it),
+// Sweep kernels alone, for timing: `sweeps` zebra sweeps that touch only scratch,
 // replayed in a graph bracketed by CUDA events on the context's stream.
-static int time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches)
+int time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches)
 {
-    Dev &d = c->d;
-    const bool mixed = c->p.precision == FVM_MIXED;
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     c->capturing = true;
-    int rc = FVM_OK;
-    for (int s = 0; s < sweeps && rc == FVM_OK; s++) {
-        if (mixed) rc = mixed_sweep_pair(c, 0);
-        else {
-            rc = launch_pois64(c, d.P, d.P2, 0, 0);
-            if (rc == FVM_OK) rc = launch_pois64(c, d.P, d.P2, 1, 0);
-        }
-    }
+    int rc = sweep_pairs(tgt_of(c), sweeps);
     c->capturing = false;
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc || e != cudaSuccess) {
@@ -844,6 +966,26 @@ static int time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long 
     return FVM_OK;
 }
 
+int calccoef_copy(fvm_ctx *c, fvm_coeffs *dout, fvm_coeffs *out)
+{
+    FVM_CUDA(c, cudaMemcpyAsync(&c->last, dout, sizeof(fvm_coeffs), cudaMemcpyDeviceToHost, c->stream));
+    FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (out) *out = c->last;
+    if (!std::isfinite(c->last.cd) || !std::isfinite(c->last.cl)) {
+        c->err = "non-finite drag or lift";
+        return FVM_ERR_NAN;
+    }
+    return FVM_OK;
+}
+
+fvm_coeffs *coef_slot(fvm_ctx *c)
+{
+    static_assert(sizeof(fvm_coeffs) <= 12 * sizeof(double), "coeff scratch");
+    return reinterpret_cast<fvm_coeffs *>(c->d.scal + 4);
+}
+
+}  // namespace
+
 int run_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches)
 {
     return time_sweeps(c, sweeps, ms_per_launch, launches);
@@ -851,7 +993,10 @@ int run_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *la
 
 int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
 {
-    RC(iter_p_async(c));
+    Tgt t = tgt_of(c);
+    LAUNCH_S(t, k_contra_vel, interior_grid(t), 128, 1);
+    RC(poisson_loop(c));
+    LAUNCH_S(t, k_bcp_ghosts, dim3((t.NI + t.NJ + 127) / 128, 1, 1), 128);
     FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, c->d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
     FVM_CUDA(c, cudaStreamSynchronize(c->stream));
     c->tm.kernel_launches += poisson_loop_kernels(c, c->h_pctl->niter);
@@ -868,62 +1013,43 @@ int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
 
 int run_correct(fvm_ctx *c)
 {
-    k_grad<<<interior_grid(c), 128, 0, c->stream>>>(c->d, +1.0, 1);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
+    Tgt t = tgt_of(c);
+    LAUNCH_S(t, k_grad, interior_grid(t), 128, +1.0, 1);
     return FVM_OK;
 }
 
 int run_iter_t(fvm_ctx *c)
 {
-    k_af_su1<<<interior_grid(c), 128, 0, c->stream>>>(c->d, FVM_FIELD_T);
+    k_af_su1<<<interior_grid(tgt_of(c)), 128, 0, c->stream>>>(c->d, FVM_FIELD_T);
     KCOUNT(c);
     FVM_LAUNCH_CHECK(c);
-    return predictor_sweeps(c, FVM_FIELD_T);
+    return predictor_sweeps(tgt_of(c), FVM_FIELD_T);
 }
 
 int run_calccoef(fvm_ctx *c, fvm_coeffs *out)
 {
-    Dev &d = c->d;
-    k_calc_rows<<<(c->NJ + 127) / 128, 128, 0, c->stream>>>(d);
-    KCOUNT(c);
-    k_cfl<<<interior_grid(c), 128, 0, c->stream>>>(d);
-    KCOUNT(c);
-    fvm_coeffs *dout = reinterpret_cast<fvm_coeffs *>(d.scal + 4);
-    static_assert(sizeof(fvm_coeffs) <= 12 * sizeof(double), "coeff scratch");
-    k_calc_final<<<1, 1, 0, c->stream>>>(d, c->rtime, dout);
-    KCOUNT(c);
-    FVM_LAUNCH_CHECK(c);
-    FVM_CUDA(c, cudaMemcpyAsync(&c->last, dout, sizeof(fvm_coeffs), cudaMemcpyDeviceToHost, c->stream));
-    FVM_CUDA(c, cudaStreamSynchronize(c->stream));
-    if (out) *out = c->last;
-    if (!std::isfinite(c->last.cd) || !std::isfinite(c->last.cl)) {
-        c->err = "non-finite drag or lift";
-        return FVM_ERR_NAN;
-    }
-    return FVM_OK;
+    Tgt t = tgt_of(c);
+    fvm_coeffs *dout = coef_slot(c);
+    LAUNCH_S(t, k_calc_rows, dim3((t.NJ + 127) / 128, 1, 1), 128);
+    LAUNCH_S(t, k_cfl, interior_grid(t), 128);
+    LAUNCH_S(t, k_calc_final, dim3(1, 1, 1), 1, c->rtime, dout);
+    return calccoef_copy(c, dout, out);
 }
 
 int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out)
 {
-    Dev &d = c->d;
     int status = FVM_OK;
     c->hist.clear();
+    Tgt t = tgt_of(c);
     for (int s = 0; s < nsteps; s++) {
-        RC(run_begin_step(c));
-        k_contra_vel<<<interior_grid(c), 128, 0, c->stream>>>(d, 0);
-        KCOUNT(c);
-        k_explicit<<<interior_grid(c), 128, 0, c->stream>>>(d, c->p.thermal);
-        KCOUNT(c);
-        FVM_LAUNCH_CHECK(c);
-        RC(predictor_sweeps(c, FVM_FIELD_U));
-        RC(predictor_sweeps(c, FVM_FIELD_V));
-        RC(run_remove_grad(c));
-        RC(iter_p_async(c));
-        RC(run_correct(c));
-        if (c->p.thermal) RC(predictor_sweeps(c, FVM_FIELD_T));
+        c->rtime = c->rtime + c->p.dt;
+        c->niter_time += 1;
+        RC(step_before_poisson(t));
+        RC(poisson_loop(c));
+        fvm_coeffs *dout = coef_slot(c);
+        RC(step_after_poisson(t, c->rtime, dout));
         fvm_coeffs co;
-        RC(run_calccoef(c, &co));
+        RC(calccoef_copy(c, dout, &co));
         c->tm.kernel_launches += poisson_loop_kernels(c, co.sweeps);
         c->tm.sweeps += co.sweeps;
         if (!std::isfinite(co.resid)) {

@@ -65,6 +65,11 @@ typedef struct fvm_params {
     int dd_positional;     /* 1 (default): DIF and ITER_P add the cross term of cell (I-1,J-1) to
                               cell (I,J), zero on row/column 1, as the reference's whole-array DD
                               operand evaluates (dif.f90:15-23, iter_p.f90:27-30); 0: cell (I,J) */
+    /* Line tiles (0 = automatic): warps per line group (1, 2 or 4) and elements per
+       thread (1..4) of the radial lines (NI-1 unknowns: Poisson and first predictor
+       factor) and of the circumferential lines (NJ-1 unknowns: second factor);
+       32 * warps * elements must cover the line.  Set both of a family or neither. */
+    int tile_r_warps, tile_r_m, tile_t_warps, tile_t_m;
 } fvm_params;
 
 /* Per-step diagnostics of CALCCOEF (calccoef.f90:9-120) plus Poisson statistics. */
@@ -167,6 +172,41 @@ int fvm_time_sweeps(struct fvm_ctx *ctx, int sweeps, double *ms_per_launch, long
 int fvm_poisson_residual_static(int ni, int nj, const double *p, const double *su, const double *ap,
                                 const double *ae, const double *aw, const double *an, const double *as,
                                 double *resid, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Batches: many independent cases (different grids, Re, Pr, dt, rotation,
+ * tolerances) advanced together, each sub-step one launch over all cases and the
+ * whole time step one CUDA graph (the Poisson loop runs on the device until the
+ * last case has converged or reached its cap).  No reference counterpart: the
+ * reference runs one case per process (Main.f90:40-118 once per run).
+ * --------------------------------------------------------------------------- */
+struct fvm_batch;
+/* params: ncases entries.  precision, thermal, iter_t_bug, res_every,
+ * refine_sweeps, device, poisson_groups and the tile fields must agree; tiles left
+ * at 0 become the automatic tile of the longest line of the batch. */
+int fvm_batch_create(int ncases, const fvm_params *params, struct fvm_batch **out);
+int fvm_batch_destroy(struct fvm_batch *b);
+const char *fvm_batch_last_error(const struct fvm_batch *b);
+/* The context of case k, owned by the batch: set it up with fvm_set_grid and
+ * fvm_init / fvm_upload_state, read it with fvm_get_array / fvm_download_state. */
+int fvm_batch_case(struct fvm_batch *b, int k, struct fvm_ctx **ctx);
+/* Line tiles shared by the cases: {radial warps, radial elements per thread,
+ * circumferential warps, circumferential elements per thread}. */
+int fvm_batch_tiles(const struct fvm_batch *b, int *tiles);
+int fvm_batch_set_tiles(struct fvm_batch *b, const int *tiles);
+/* Times every tile that covers the batch's lines on the batch itself (`sweeps`
+ * replays of the batched Poisson sweep for the radial family, of the batched
+ * circumferential predictor sweep for the other) and keeps the fastest.  Needs
+ * every case's grid; the flow state is left unchanged.  tiles (4 ints) and ms
+ * (2 doubles: best time per sweep of each family) may be NULL. */
+int fvm_batch_autotune(struct fvm_batch *b, int sweeps, int *tiles, double *ms);
+/* Average time of one batched Poisson sweep (both colours, state unchanged). */
+int fvm_batch_time_sweeps(struct fvm_batch *b, int sweeps, double *ms_per_sweep);
+/* nsteps time steps of every case.  out (may be NULL) receives nsteps*ncases
+ * records, step-major (out[s*ncases + k]); each case's fvm_history holds its own.
+ * Returns FVM_ERR_NOCONV if any case hit its sweep cap. */
+int fvm_batch_step(struct fvm_batch *b, int nsteps, fvm_coeffs *out);
+int fvm_batch_get_timing(const struct fvm_batch *b, fvm_timing *out);
 
 #ifdef __cplusplus
 }

@@ -41,12 +41,17 @@ def make_oracle(case, order=oracle.GPU, res_every=2):
     return o
 
 
-def make_gpu(case, precision=capi.FP64, res_every=2, refine_sweeps=4, adi_refine=2):
+def case_params(case, precision=capi.FP64, res_every=2, refine_sweeps=4, adi_refine=2, **extra):
     g = case["g"]
-    p = capi.default_params(ni=g.ni, nj=g.nj, re=case["re"], pr=case["pr"], dt=case["dt"],
-                            vel_rot=case["vel_rot"], resimax=case["resimax"], nswpp=case["nswpp"],
-                            thermal=int(case["thermal"]), precision=precision, res_every=res_every,
-                            refine_sweeps=refine_sweeps, adi_refine=adi_refine)
+    return capi.default_params(ni=g.ni, nj=g.nj, re=case["re"], pr=case["pr"], dt=case["dt"],
+                               vel_rot=case["vel_rot"], resimax=case["resimax"], nswpp=case["nswpp"],
+                               thermal=int(case["thermal"]), precision=precision, res_every=res_every,
+                               refine_sweeps=refine_sweeps, adi_refine=adi_refine, **extra)
+
+
+def make_gpu(case, precision=capi.FP64, res_every=2, refine_sweeps=4, adi_refine=2, **extra):
+    g = case["g"]
+    p = case_params(case, precision, res_every, refine_sweeps, adi_refine, **extra)
     ctx = capi.Context(p)
     ctx.set_grid(g.xg, g.yg)
     ctx.init(case["du"], case["dv"])

@@ -44,3 +44,22 @@ def test_create_rejects_bad_parameters_without_a_gpu():
     assert L.fvm_create(None, ctypes.byref(h)) == capi.FVM_ERR_ARG
     assert L.fvm_destroy(None) == capi.FVM_ERR_ARG
     assert L.fvm_step(None, 1, None) == capi.FVM_ERR_ARG
+
+
+def test_batch_rejects_mismatched_options_without_a_gpu():
+    L = capi.load()
+    h = ctypes.c_void_p()
+    ps = (capi.Params * 2)(capi.default_params(), capi.default_params(precision=capi.MIXED))
+    assert L.fvm_batch_create(2, ps, ctypes.byref(h)) == capi.FVM_ERR_ARG
+    assert L.fvm_batch_create(0, ps, ctypes.byref(h)) == capi.FVM_ERR_ARG
+    assert L.fvm_batch_destroy(None) == capi.FVM_ERR_ARG
+    assert L.fvm_batch_step(None, 1, None) == capi.FVM_ERR_ARG
+
+
+def test_create_rejects_a_tile_that_does_not_cover_the_line():
+    L = capi.load()
+    h = ctypes.c_void_p()
+    p = capi.default_params(ni=97, tile_r_warps=1, tile_r_m=2)     # 64 < 96 radial cells
+    assert L.fvm_create(ctypes.byref(p), ctypes.byref(h)) == capi.FVM_ERR_ARG
+    p = capi.default_params(tile_r_warps=3, tile_r_m=1)
+    assert L.fvm_create(ctypes.byref(p), ctypes.byref(h)) == capi.FVM_ERR_ARG
