@@ -299,6 +299,88 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------------------------
+# sweep of 64 ragged cases (fvm_batch_*), sharded over the ranks by estimated cost
+# ---------------------------------------------------------------------------------
+SWEEP = dict(name="sweep64-ragged-mixed", n=64, seed=0, resimax=1e-10, nswpp=2048, refine_sweeps=32)
+
+
+def run_sweep_bench(args):
+    import numpy as np
+    import torch
+    from fvm_gb300 import batch, capi, dist
+
+    rank, world = dist.init("nccl")
+    local = dist.rank_world()[2]
+    torch.cuda.set_device(local)
+    sw = dict(SWEEP)
+    specs = batch.sweep_cases(sw["n"], seed=sw["seed"])
+    parts = batch.partition([batch.case_cost(s) for s in specs], world)
+    mine = [specs[k] for k in parts[rank]]
+    kw = dict(resimax=sw["resimax"], nswpp=sw["nswpp"], refine_sweeps=sw["refine_sweeps"], device=local)
+    t0 = time.perf_counter()
+    b = batch.build_batch(mine, capi.MIXED, autotune_sweeps=20, **kw)
+    setup_s = time.perf_counter() - t0
+    b.step(args.warmup)
+    tl0 = b.timing()["kernel_launches"]
+    dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    t0 = time.perf_counter()
+    recs = b.step(args.steps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    clocks = clk.stop()
+    dist.barrier()
+    dt_max = dist.max_over_ranks(dt, device="cuda")
+    launches = b.timing()["kernel_launches"] - tl0
+    units = sum(s.cells for s in specs) * args.steps
+    value = units / dt_max / 1e6
+    sweeps = [r["sweeps"] for r in recs[-1]]
+    tiles_used = list(b.tiles())
+    # the same cases one by one (separate contexts, same tiles), rank 0 of a
+    # single-GPU run: warm-up, then 2 timed steps per case
+    one = None
+    if world == 1:
+        tiles = b.tiles()
+        t_one, ones_equal = 0.0, True
+        tk = dict(tile_r_warps=tiles[0], tile_r_m=tiles[1], tile_t_warps=tiles[2], tile_t_m=tiles[3])
+        for k, s in enumerate(mine):
+            ctx = capi.Context(batch.case_params(s, capi.MIXED, **kw, **tk))
+            g, du, dv = batch.case_inputs(s)
+            ctx.set_grid(g.xg, g.yg)
+            ctx.init(du, dv)
+            ctx.step(args.warmup)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            ctx.step(2)
+            torch.cuda.synchronize()
+            t_one += time.perf_counter() - t1
+            ctx.close()
+        one = {"value": sum(s.cells for s in mine) * 2 / t_one / 1e6, "unit": "Mcell-steps/s",
+               "note": "same cases as independent contexts stepped one after another, 2 steps each"}
+    b.close()
+    out = {"metric": METRIC, "workload": sw["name"], "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt_max / args.steps,
+           "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64+f32",
+           "data": "synthetic",
+           "config": {"workload": sw["name"], "cases": len(specs), "cells": sum(s.cells for s in specs),
+                      "grids": "theta cells uniform in {64..256} step 16, radial cells uniform in 48..192, "
+                               "Re log-uniform in [60, 300], dt 0.004, seeded",
+                      "poisson": f"zebra line GS to scaled-L1 {sw['resimax']:g}, cap NSWPP={sw['nswpp']}",
+                      "sweeps_per_step": {"min": min(sweeps), "max": max(sweeps)},
+                      "tiles": {"radial": tiles_used[:2], "circumferential": tiles_used[2:],
+                                "chosen_by": "autotuner (timed on this batch)"},
+                      "partition": [len(p) for p in parts],
+                      "setup_s_rank": setup_s,
+                      "l2": "inputs larger than L2 (about 0.5 GB of case state)"},
+           "one_by_one": one, "gpu_launches": int(launches), "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    dist.finalize()
+
+
+# ---------------------------------------------------------------------------------
 # reference arm
 # ---------------------------------------------------------------------------------
 def run_reference(args):
@@ -376,11 +458,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--parts", choices=["all", "mixed"], default="all",
                     help="'mixed' times only the headline path (for profiler runs)")
+    ap.add_argument("--workload", choices=["cylinder2d", "sweep64"], default="cylinder2d",
+                    help="sweep64: 64 ragged cases advanced as batches, sharded over the ranks")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "sweep64":
+        run_sweep_bench(args)
     else:
         run_ours(args)
 
