@@ -23,7 +23,7 @@ STATUS_NAMES = {0: "FVM_OK", 1: "FVM_ERR_ARG", 2: "FVM_ERR_CUDA", 3: "FVM_ERR_NO
 # Every symbol include/fvm.h declares (checked by the CPU tests).
 EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", "fvm_set_grid",
            "fvm_init", "fvm_upload_state", "fvm_download_state", "fvm_get_array", "fvm_set_array",
-           "fvm_set_time", "fvm_begin_step", "fvm_contra_vel", "fvm_nl", "fvm_dif", "fvm_p_source",
+           "fvm_set_time", "fvm_set_controls", "fvm_adjoint_drag_grad", "fvm_adjoint_vjp", "fvm_begin_step", "fvm_contra_vel", "fvm_nl", "fvm_dif", "fvm_p_source",
            "fvm_iter_u", "fvm_iter_v", "fvm_remove_grad", "fvm_iter_p", "fvm_correct", "fvm_iter_t",
            "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize", "fvm_get_stream",
            "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps", "fvm_poisson_residual_static",
@@ -102,6 +102,9 @@ def load(build_if_missing: bool = True):
     L.fvm_get_array.argtypes = [V, ctypes.c_char_p, D]
     L.fvm_set_array.argtypes = [V, ctypes.c_char_p, D]
     L.fvm_set_time.argtypes = [V, ctypes.c_double, ctypes.c_int]
+    L.fvm_set_controls.argtypes = [V, ctypes.c_double, D]
+    L.fvm_adjoint_drag_grad.argtypes = [V, ctypes.c_int, ctypes.c_int, D, D, D]
+    L.fvm_adjoint_vjp.argtypes = [V, D, D, D, D, D, D]
     for f in ("fvm_begin_step", "fvm_contra_vel", "fvm_p_source", "fvm_iter_u", "fvm_iter_v",
               "fvm_remove_grad", "fvm_correct", "fvm_iter_t", "fvm_synchronize"):
         getattr(L, f).argtypes = [V]
@@ -221,6 +224,32 @@ class Context:
 
     def set_time(self, t, niter=0):
         self._ok(self.L.fvm_set_time(self.h, t, niter))
+
+    def set_controls(self, omega=0.0, blow=None):
+        """Wall rotation rate and wall-normal blowing speeds (NJ-1 values)."""
+        b = None if blow is None else _arr(blow, self.nj - 1)
+        self._ok(self.L.fvm_set_controls(self.h, omega, _dp(b)))
+
+    def adjoint_drag_grad(self, window, ckpt=50):
+        """Runs `window` steps from the current state; returns (J, dJ/domega,
+        dJ/dblow) with J the mean drag coefficient over the window."""
+        J = ctypes.c_double()
+        dw = ctypes.c_double()
+        db = np.zeros(self.nj - 1)
+        self._ok(self.L.fvm_adjoint_drag_grad(self.h, window, ckpt, ctypes.byref(J), ctypes.byref(dw), _dp(db)),
+                 allow=(FVM_ERR_NOCONV,))
+        return J.value, dw.value, db
+
+    def adjoint_vjp(self, lam):
+        """One step transposed at the current state: lam maps U, V, P, NLX, NLY to
+        adjoints of the state after the step (arrays shaped like get()); returns the
+        adjoints of the state before it and the control adjoints (rotation, blowing)."""
+        names = ("U", "V", "P", "NLX", "NLY")
+        arrs = [np.ascontiguousarray(lam[nm], dtype=np.float64).ravel().copy() for nm in names]
+        ctrl = np.zeros(self.nj)
+        self._ok(self.L.fvm_adjoint_vjp(self.h, *[_dp(a) for a in arrs], _dp(ctrl)))
+        out = {nm: a.reshape(self.nj + 1, self.ni + 1) for nm, a in zip(names, arrs)}
+        return out, ctrl[0], ctrl[1:]
 
     # reference call points -----------------------------------------------------
     def begin_step(self): self._ok(self.L.fvm_begin_step(self.h))

@@ -116,6 +116,7 @@ int fvm_destroy(fvm_ctx *c)
 {
     if (!c) return FVM_ERR_ARG;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    fvm::adj_destroy(c);
     if (c->pgraph) cudaGraphExecDestroy(c->pgraph);
     if (c->slab) cudaFree(c->slab);
     if (c->h_pctl) cudaFreeHost(c->h_pctl);
@@ -208,6 +209,34 @@ int fvm_set_time(fvm_ctx *c, double rtime, int niter_time)
     c->rtime = rtime;
     c->niter_time = niter_time;
     return FVM_OK;
+}
+
+int fvm_adjoint_drag_grad(fvm_ctx *c, int window, int ckpt, double *J, double *dJ_domega, double *dJ_dblow)
+{
+    int r = need_ready(c);
+    if (r) return r;
+    if (window < 1 || ckpt < 1) return bad(c, "window and checkpoint interval must be positive");
+    return fvm::run_adjoint(c, window, ckpt, J, dJ_domega, dJ_dblow);
+}
+
+int fvm_adjoint_vjp(fvm_ctx *c, double *lu, double *lv, double *lp, double *lnlx, double *lnly, double *dctrl)
+{
+    int r = need_ready(c);
+    if (r) return r;
+    if (!lu || !lv || !lp || !lnlx || !lnly) return bad(c, "null adjoint array");
+    double *lam[5] = {lu, lv, lp, lnlx, lnly};
+    return fvm::run_adjoint_vjp(c, lam, dctrl);
+}
+
+int fvm_set_controls(fvm_ctx *c, double omega, const double *blow)
+{
+    if (!c) return FVM_ERR_ARG;
+    if (!c->grid_set) return bad(c, "fvm_set_controls needs the grid");
+    if (!std::isfinite(omega)) return bad(c, "non-finite rotation rate");
+    if (blow)
+        for (int j = 0; j < c->NJ - 1; j++)
+            if (!std::isfinite(blow[j])) return bad(c, "non-finite blowing speed");
+    return fvm::setup_controls(c, omega, blow);
 }
 
 #define READY()                          \

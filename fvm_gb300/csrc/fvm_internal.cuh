@@ -92,6 +92,7 @@ struct Dev {
     double *RJDT;          // (2*RE)*DJAC/DT  and for Pe:
     double *PJDT;          // (2*PE)*DJAC/DT
     double *UFW, *VFW, *TFW;  // wall boundary values per j (constant)
+    double *BLOW, *WB;        // wall blowing speed per j (control) and its face-flux weight
     double *FFU, *FFV, *FFT;  // far-field boundary values per j (per step)
     // state
     double *U, *V, *P, *T, *U_N, *V_N, *T_N;
@@ -123,6 +124,8 @@ __device__ __forceinline__ const Dev &dev_of(const DevTable &t) { return t.devs[
 
 }  // namespace fvm
 
+struct fvm_adj;   // adjoint storage (fvm_adjoint.cu), created on first use
+
 struct fvm_ctx {
     fvm_params p{};
     int NI = 0, NJ = 0, NI1 = 0, n = 0;
@@ -147,6 +150,7 @@ struct fvm_ctx {
     int span_launches = 0;                        // sweep kernels inside the span
     bool capturing = false;
     fvm_timing tm{};
+    fvm_adj *adj = nullptr;
 };
 
 // Count one kernel launch of the context (into the graph being captured, if any).
@@ -203,6 +207,7 @@ inline void with_src(const Tgt &t, F &&f)
 Tgt tgt_of(fvm_ctx *c);
 int setup_allocate(fvm_ctx *c);
 int setup_factors(fvm_ctx *c);
+int setup_controls(fvm_ctx *c, double omega, const double *blow);
 int setup_grid(fvm_ctx *c);
 int setup_init(fvm_ctx *c, const double *du, const double *dv);
 int run_begin_step(fvm_ctx *c);
@@ -225,6 +230,10 @@ int poisson_bodies(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond, 
 int step_after_poisson(const Tgt &t, double rtime, fvm_coeffs *dout);
 int sweep_pairs(const Tgt &t, int sweeps);
 int launch_batch_tick(const Tgt &t, BatchCtl *b);
+// discrete adjoint (fvm_adjoint.cu)
+int run_adjoint(fvm_ctx *c, int window, int ckpt, double *J, double *dJ_domega, double *dJ_dblow);
+int run_adjoint_vjp(fvm_ctx *c, double *const *lam, double *dctrl);
+void adj_destroy(fvm_ctx *c);
 int theta_pairs(const Tgt &t, int field, int sweeps);
 int predictor_sweeps(const Tgt &t, int field);
 // mixed precision (fvm_mixed.cu)

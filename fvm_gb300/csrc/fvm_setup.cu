@@ -78,7 +78,7 @@ void carve(Bump &b, fvm_ctx *c, int nblk)
                       &d.Q12, &d.Q22, &d.DE, &d.DW, &d.DN, &d.DS, &d.THETA, &d.AREA, &d.JQ12,
                       &d.JXE, &d.JYE, &d.RJDT, &d.PJDT, &d.CNE, &d.CSE, &d.CNW, &d.CSW};
     for (auto p : geo) *p = b.take<double>(n);
-    double **perj[] = {&d.UFW, &d.VFW, &d.TFW, &d.FFU, &d.FFV, &d.FFT};
+    double **perj[] = {&d.UFW, &d.VFW, &d.TFW, &d.FFU, &d.FFV, &d.FFT, &d.BLOW, &d.WB};
     for (auto p : perj) *p = b.take<double>(nj1);
     double **st[] = {&d.U, &d.V, &d.P, &d.P2, &d.T, &d.U_N, &d.V_N, &d.T_N, &d.NLX, &d.NLY, &d.ADV,
                      &d.NLX_NM1, &d.NLY_NM1, &d.ADV_NM1, &d.DIFX, &d.DIFY, &d.DIFT, &d.S_U,
@@ -310,9 +310,34 @@ __global__ void k_wall_values(Dev d)
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j > d.NJ) return;
     double th = d.THETA[IDX(0, j)];
-    d.UFW[j] = d.vel_rot * (-sin(th));   // bcu.f90:13
-    d.VFW[j] = d.vel_rot * cos(th);      // bcv.f90:13
+    // bcu.f90:13, bcv.f90:13, plus the wall-normal blowing control (zero unless set)
+    const double ct = cos(th), st = sin(th), b = d.BLOW[j];
+    d.UFW[j] = d.vel_rot * (-st) + b * ct;
+    d.VFW[j] = d.vel_rot * ct + b * st;
     d.TFW[j] = d.t_wall;                 // bct.f90:13
+    // face value of J*(xi_x cos th + xi_y sin th) between the ghost and first cells:
+    // the wall face flux UW(1,j) per unit blowing speed
+    const int c0 = IDX(0, j), c1 = IDX(1, j);
+    d.WB[j] = 0.5 * __dadd_rn(__dmul_rn(d.DJAC[c0], __dadd_rn(__dmul_rn(d.XIX[c0], ct), __dmul_rn(d.XIY[c0], st))),
+                              __dmul_rn(d.DJAC[c1], __dadd_rn(__dmul_rn(d.XIX[c1], ct), __dmul_rn(d.XIY[c1], st))));
+}
+
+// Wall controls: rotation rate (VEL_ROT) and blowing speeds, then the wall values.
+int setup_controls(fvm_ctx *c, double omega, const double *blow)
+{
+    Dev &d = c->d;
+    c->p.vel_rot = omega;
+    d.vel_rot = omega;
+    std::vector<double> b(c->NJ + 1, 0.0);
+    if (blow)
+        for (int j = 1; j <= c->NJ - 1; j++) b[j] = blow[j - 1];
+    FVM_CUDA(c, cudaMemcpyAsync(d.BLOW, b.data(), sizeof(double) * (c->NJ + 1), cudaMemcpyHostToDevice, c->stream));
+    FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+    k_wall_values<<<(c->NJ + 1 + 127) / 128, 128, 0, c->stream>>>(d);
+    FVM_LAUNCH_CHECK(c);
+    if (c->pgraph) cudaGraphExecDestroy(c->pgraph);
+    c->pgraph = nullptr;
+    return FVM_OK;
 }
 
 // ---------------------------------------------------------------------------------

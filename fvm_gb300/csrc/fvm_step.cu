@@ -69,7 +69,8 @@ __global__ void k_contra_vel(const __grid_constant__ S src, int with_poisson)
     int c = IDX(i, j), e = IDX(i + 1, j), w = IDX(i - 1, j), nn = IDX(i, j + 1), s = IDX(i, j - 1);
     double ju1 = J[c] * u1_at(d, c), ju2 = J[c] * u2_at(d, c);
     double ue = 0.5 * (ju1 + J[e] * u1_at(d, e));
-    double uw = (i == 1) ? 0.0 : 0.5 * (ju1 + J[w] * u1_at(d, w));
+    // UW(1,j) = 0 in the reference (contra_vel.f90:125); with wall blowing, its flux
+    double uw = (i == 1) ? d.WB[j] * d.BLOW[j] : 0.5 * (ju1 + J[w] * u1_at(d, w));
     double vn = 0.5 * (ju2 + J[nn] * u2_at(d, nn));
     double vs = 0.5 * (ju2 + J[s] * u2_at(d, s));
     d.UE[c] = ue;

@@ -104,6 +104,32 @@ int fvm_download_state(struct fvm_ctx *ctx, double *u, double *v, double *p, dou
 int fvm_get_array(struct fvm_ctx *ctx, const char *name, double *out);
 int fvm_set_array(struct fvm_ctx *ctx, const char *name, const double *in);
 int fvm_set_time(struct fvm_ctx *ctx, double rtime, int niter_time);
+/* Wall controls (no reference counterpart beyond VEL_ROT): rotation rate omega
+ * (the reference's VEL_ROT, bcu.f90:13) and a wall-normal blowing speed per wall
+ * cell, blow[J-1] for J=1..NJ-1 (NULL: none).  The wall velocity of cell J is
+ * omega*(-sin th, cos th) + blow*(cos th, sin th) with th = THETA(0,J), and the
+ * wall face flux UW(1,J) (zero in contra_vel.f90:125) becomes blow times the face
+ * value of J*(xi_x cos th + xi_y sin th).  With blow = 0 the step is the
+ * reference's. */
+int fvm_set_controls(struct fvm_ctx *ctx, double omega, const double *blow);
+
+/* Discrete adjoint (no reference counterpart).  From the current state, runs
+ * `window` steps (the state advances, as fvm_step would) and returns
+ * J = mean over those steps of the drag coefficient CALCCOEF reports, with its
+ * exact gradient for the discrete step (Poisson taken as converged) with respect
+ * to the rotation rate (dJ_domega) and the NJ-1 blowing speeds (dJ_dblow), the
+ * controls held fixed over the window.  The state is checkpointed every `ckpt`
+ * steps and each segment recomputed for the reverse pass.  Any output may be
+ * NULL.  Returns FVM_ERR_NOCONV if a forward step hit its sweep cap. */
+int fvm_adjoint_drag_grad(struct fvm_ctx *ctx, int window, int ckpt, double *J, double *dJ_domega,
+                          double *dJ_dblow);
+/* Transpose of one step at the current state (the state is left unchanged): the
+ * five host arrays (U, V, P, NLX, NLY adjoints, full-array storage) hold on
+ * entry the adjoint of the state after the step and on exit that of the state
+ * before it; dctrl (may be NULL) receives 1 + (NJ-1) control adjoints
+ * (rotation, then blowing). */
+int fvm_adjoint_vjp(struct fvm_ctx *ctx, double *lu, double *lv, double *lp, double *lnlx, double *lnly,
+                    double *dctrl);
 
 /* One call point each of the reference time loop (Main.f90:48-114). */
 int fvm_begin_step(struct fvm_ctx *ctx);   /* Main.f90:48-54: time advance, U_N=U, V_N=V, T_N=T */

@@ -62,6 +62,7 @@ def lib():
         L.orc_time.restype = ctypes.c_double
         L.orc_time.argtypes = [ctypes.c_void_p]
         L.orc_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        L.orc_set_controls.argtypes = [ctypes.c_void_p, ctypes.c_double, P]
         L.orc_sum_area.restype = ctypes.c_double
         L.orc_sum_area.argtypes = [ctypes.c_void_p]
         L.orc_iter_p.restype = ctypes.c_int
@@ -118,6 +119,24 @@ class Oracle:
 
     def call(self, name):
         return getattr(lib(), "orc_" + name)(self._h)
+
+    def set_controls(self, omega=0.0, blow=None):
+        """Wall rotation rate and wall-normal blowing speeds (NJ-1 values)."""
+        b = None if blow is None else np.ascontiguousarray(blow, dtype=np.float64).ravel()
+        if b is not None and b.size != self.nj - 1:
+            raise ValueError(f"blow needs {self.nj - 1} values")
+        lib().orc_set_controls(self._h, ctypes.c_double(omega), None if b is None else _dptr(b))
+
+    STATE = ("U", "V", "P", "T", "U_N", "V_N", "T_N", "NLX", "NLY", "ADV", "NLX_NM1", "NLY_NM1", "ADV_NM1")
+
+    def save_state(self):
+        return {nm: self.array(nm).copy() for nm in self.STATE}, self.time
+
+    def restore_state(self, saved):
+        arrs, t = saved
+        for nm, a in arrs.items():
+            self.array(nm)[...] = a
+        self.set_time(t)
 
     def array(self, name) -> np.ndarray:
         p = lib().orc_array(self._h, name.encode())

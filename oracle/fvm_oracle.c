@@ -30,6 +30,8 @@ struct orc {
     double *U1, *U2, *UE, *UW, *VN, *VS, *AP, *AE, *AW, *AN, *AS, *SU, *DD;
     /* line work arrays */
     double *la, *lb, *lc, *ld, *lx, *lz, *lw, *lu, *lbb;
+    /* wall controls (no reference counterpart): wall-normal blowing speed per J */
+    double *BLOW;
     orc_coeffs co;
 };
 
@@ -64,7 +66,8 @@ orc *orc_create(const orc_params *p)
     o->la = zalloc(m); o->lb = zalloc(m); o->lc = zalloc(m);
     o->ld = zalloc(m); o->lx = zalloc(m); o->lz = zalloc(m);
     o->lw = zalloc(m); o->lu = zalloc(m); o->lbb = zalloc(m);
-    if (!o->la || !o->lb || !o->lc || !o->ld || !o->lx || !o->lz || !o->lw || !o->lu || !o->lbb) {
+    o->BLOW = zalloc(p->nj + 1);
+    if (!o->la || !o->lb || !o->lc || !o->ld || !o->lx || !o->lz || !o->lw || !o->lu || !o->lbb || !o->BLOW) {
         orc_destroy(o);
         return NULL;
     }
@@ -80,7 +83,7 @@ void orc_destroy(orc *o)
                       o->ADV, o->NLX_NM1, o->NLY_NM1, o->ADV_NM1, o->DIFX, o->DIFY, o->DIFT,
                       o->S_U, o->S_V, o->U1, o->U2, o->UE, o->UW, o->VN, o->VS, o->AP, o->AE,
                       o->AW, o->AN, o->AS, o->SU, o->DD, o->la, o->lb, o->lc, o->ld, o->lx, o->lz,
-                      o->lw, o->lu, o->lbb};
+                      o->lw, o->lu, o->lbb, o->BLOW};
     for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); k++) free(arrs[k]);
     free(o);
 }
@@ -225,8 +228,8 @@ static void bc_field(orc *o, int kind, double *phi, const double *phin)
     for (int j = 1; j <= NJ - 1; j++) {
         double th = o->THETA[ID(0, j)];
         double f;
-        if (kind == BC_U) f = o->p.vel_rot * (-sin(th));
-        else if (kind == BC_V) f = o->p.vel_rot * cos(th);
+        if (kind == BC_U) f = o->p.vel_rot * (-sin(th)) + o->BLOW[j] * cos(th);
+        else if (kind == BC_V) f = o->p.vel_rot * cos(th) + o->BLOW[j] * sin(th);
         else f = o->p.t_wall;
         int c1 = ID(1, j);
         o->AP[c1] = o->AP[c1] + o->AW[c1];
@@ -336,6 +339,30 @@ int orc_init(orc *o, const double *du, const double *dv)
 }
 
 /* ------------------------------------------------------------------------- */
+/* Wall controls (no reference counterpart)                                   */
+/* ------------------------------------------------------------------------- */
+/* Wall rotation rate omega (the reference's VEL_ROT, bcu.f90:13) and a
+ * wall-normal blowing speed b_J per wall cell J=1..NJ-1: the wall velocity of
+ * cell J becomes omega*(-sin th, cos th) + b_J*(cos th, sin th), th = THETA(0,J),
+ * and the wall face flux UW(1,J), zero in the reference (contra_vel.f90:125), is
+ * b_J times the face value of J*(xi_x cos th + xi_y sin th) averaged over the
+ * ghost and first cells.  With b = 0 the step is the reference's. */
+void orc_set_controls(orc *o, double omega, const double *blow)
+{
+    o->p.vel_rot = omega;
+    for (int j = 0; j <= o->NJ; j++) o->BLOW[j] = 0.0;
+    if (blow)
+        for (int j = 1; j <= o->NJ - 1; j++) o->BLOW[j] = blow[j - 1];
+}
+
+static double wall_flux(const orc *o, int j)
+{
+    const double th = o->THETA[ID(0, j)], ct = cos(th), st = sin(th);
+    const int c0 = ID(0, j), c1 = ID(1, j);
+    return 0.5 * (o->DJAC[c0] * (o->XIX[c0] * ct + o->XIY[c0] * st) + o->DJAC[c1] * (o->XIX[c1] * ct + o->XIY[c1] * st));
+}
+
+/* ------------------------------------------------------------------------- */
 /* Explicit operators                                                         */
 /* ------------------------------------------------------------------------- */
 /* CONTRA_VEL, FLAG=0 (contra_vel.f90:9-21,125) */
@@ -355,7 +382,7 @@ void orc_contra_vel(orc *o)
             o->VN[c] = 0.5 * (J[c] * U2[c] + J[ID(i, j + 1)] * U2[ID(i, j + 1)]);
             o->VS[c] = 0.5 * (J[c] * U2[c] + J[ID(i, j - 1)] * U2[ID(i, j - 1)]);
         }
-    for (int j = 1; j <= NJ - 1; j++) o->UW[ID(1, j)] = 0.0;
+    for (int j = 1; j <= NJ - 1; j++) o->UW[ID(1, j)] = wall_flux(o, j) * o->BLOW[j];
 }
 
 /* NL (nl.f90:21-27): face-flux advection */

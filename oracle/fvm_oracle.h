@@ -86,6 +86,11 @@ void orc_correct(orc *o);         /* Main.f90:97-107 */
 void orc_iter_t(orc *o);          /* Main.f90:110-111 */
 void orc_calccoef(orc *o);        /* calccoef.f90 */
 
+/* Wall controls, no reference counterpart: rotation rate omega (VEL_ROT) and a
+ * wall-normal blowing speed per wall cell (blow[J-1] for J=1..NJ-1; NULL = 0),
+ * entering the wall velocity of BCU/BCV and the wall face flux UW(1,J). */
+void orc_set_controls(orc *o, double omega, const double *blow);
+
 /* Raw access to any named array (NULL if unknown).  Names: "U","V","P","T",
  * "U_N","V_N","T_N","NLX","NLY","ADV","NLX_NM1","NLY_NM1","ADV_NM1","DIFX",
  * "DIFY","DIFT","S_U","S_V","UE","UW","VN","VS","X","Y","XG","YG","XIX","XIY",
