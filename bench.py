@@ -299,6 +299,88 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------------------------
+# discrete adjoint: d(mean Cd over a window)/d(rotation, blowing) on the 128 x 96 grid
+# ---------------------------------------------------------------------------------
+ADJOINT = dict(name="adjoint-cylinder2d-re100-128x96", n_theta=128, n_r=96, re=100.0, pr=0.71, dt=0.005,
+               resimax=1e-10, nswpp=100000, amp=1e-3, seed=0, dr1=0.005, r_out=50.0, window=500, ckpt=50,
+               omega=0.0, blow_sigma=0.01)
+
+
+def adjoint_measure(spinup, precision, device, fd_check=True):
+    """Spin-up, then the window forward alone and the adjoint call (its own
+    forward pass, the recomputation of every segment and the reverse pass), both
+    timed; the rotation gradient is compared with a central difference (h=1e-6) of
+    the same solver when fd_check."""
+    import numpy as np
+    import torch
+    from fvm_gb300 import capi
+    a = dict(ADJOINT)
+    g, du, dv = case_inputs(a)
+    p = capi.default_params(ni=g.ni, nj=g.nj, re=a["re"], pr=a["pr"], dt=a["dt"], resimax=a["resimax"],
+                            nswpp=a["nswpp"], thermal=0, precision=precision, res_every=8, refine_sweeps=16,
+                            device=device)
+    ctx = capi.Context(p)
+    ctx.set_grid(g.xg, g.yg)
+    ctx.init(du, dv)
+    blow = a["blow_sigma"] * np.random.default_rng(a["seed"]).standard_normal(g.nj - 1)
+    ctx.set_controls(a["omega"], blow)
+    ctx.step(spinup)
+    start = {nm: ctx.get(nm) for nm in ("U", "V", "P", "T", "NLX", "NLY", "ADV")}
+
+    def restore():
+        ctx.upload(start["U"], start["V"], start["P"], start["T"], start["NLX"], start["NLY"], start["ADV"])
+
+    def window_cd(omega):
+        restore()
+        ctx.set_controls(omega, blow)
+        ctx.step(a["window"])
+        return float(np.mean([h["cd"] for h in ctx.history(a["window"])]))
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    j_fwd = window_cd(a["omega"])
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    restore()
+    ctx.set_controls(a["omega"], blow)
+    t0 = time.perf_counter()
+    J, dw, db = ctx.adjoint_drag_grad(a["window"], a["ckpt"])
+    torch.cuda.synchronize()
+    t_adj = time.perf_counter() - t0
+    out = {"J": J, "dJ_domega": dw, "dJ_dblow_norm": float(np.linalg.norm(db)), "forward_s": t_fwd,
+           "adjoint_s": t_adj, "adjoint_over_forward": t_adj / t_fwd, "J_vs_forward": abs(J - j_fwd) / abs(j_fwd),
+           "spinup_steps": spinup}
+    if fd_check:
+        h = 1e-6
+        fd = (window_cd(a["omega"] + h) - window_cd(a["omega"] - h)) / (2 * h)
+        out["fd_dJ_domega"] = fd
+        out["rel_err_vs_fd"] = abs(dw - fd) / abs(fd)
+    ctx.close()
+    return out
+
+
+def run_adjoint_bench(args):
+    import torch
+    from fvm_gb300 import capi, dist
+    rank, world = dist.init("nccl")
+    local = dist.rank_world()[2]
+    torch.cuda.set_device(local)
+    res = {nm: adjoint_measure(args.spinup, prec, local) for nm, prec in (("fp64", capi.FP64), ("mixed", capi.MIXED))}
+    a = ADJOINT
+    out = {"metric": METRIC, "workload": a["name"], "value": res["fp64"]["adjoint_over_forward"],
+           "unit": "adjoint/forward time", "n_gpus": world, "higher_is_better": False, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": a["name"], "grid": f"{a['n_theta']} theta x {a['n_r']} r", "re": a["re"],
+                      "dt": a["dt"], "window": a["window"], "checkpoint_every": a["ckpt"],
+                      "spinup_steps": args.spinup, "poisson": f"scaled-L1 {a['resimax']:g}",
+                      "controls": "rotation omega=0 and 128 blowing speeds ~ N(0, 0.01^2), seeded"},
+           "fp64": res["fp64"], "mixed": res["mixed"]}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    dist.finalize()
+
+
+# ---------------------------------------------------------------------------------
 # sweep of 64 ragged cases (fvm_batch_*), sharded over the ranks by estimated cost
 # ---------------------------------------------------------------------------------
 SWEEP = dict(name="sweep64-ragged-mixed", n=64, seed=0, resimax=1e-10, nswpp=2048, refine_sweeps=32)
@@ -458,8 +540,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--parts", choices=["all", "mixed"], default="all",
                     help="'mixed' times only the headline path (for profiler runs)")
-    ap.add_argument("--workload", choices=["cylinder2d", "sweep64"], default="cylinder2d",
-                    help="sweep64: 64 ragged cases advanced as batches, sharded over the ranks")
+    ap.add_argument("--workload", choices=["cylinder2d", "sweep64", "adjoint"], default="cylinder2d",
+                    help="sweep64: 64 ragged cases advanced as batches, sharded over the ranks; "
+                         "adjoint: window-drag gradient on the 128x96 grid")
+    ap.add_argument("--spinup", type=int, default=2000, help="adjoint workload: steps before the window")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -467,6 +551,8 @@ def main():
         run_reference(args)
     elif args.workload == "sweep64":
         run_sweep_bench(args)
+    elif args.workload == "adjoint":
+        run_adjoint_bench(args)
     else:
         run_ours(args)
 

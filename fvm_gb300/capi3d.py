@@ -1,0 +1,147 @@
+"""ctypes binding of the 3-D LES C-ABI (include/fvm3d.h).  Field arrays are numpy
+arrays shaped (NK+1, NJ+1, NI+1): a[k, j, i] is the reference's (I, J, K)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+
+EXPORTS = ["fvm3_default_params", "fvm3_create", "fvm3_destroy", "fvm3_last_error", "fvm3_set_grid", "fvm3_init",
+           "fvm3_step", "fvm3_get_array", "fvm3_set_array", "fvm3_sgs", "fvm3_time_sweeps", "fvm3_get_stream"]
+
+
+class Params3(ctypes.Structure):
+    _fields_ = [("ni", ctypes.c_int), ("nj", ctypes.c_int), ("nk", ctypes.c_int),
+                ("re", ctypes.c_double), ("pr", ctypes.c_double), ("dt", ctypes.c_double),
+                ("tin", ctypes.c_double), ("t_wall", ctypes.c_double), ("resimax", ctypes.c_double),
+                ("nswpp", ctypes.c_int), ("use_les", ctypes.c_int), ("les_zavg", ctypes.c_int),
+                ("thermal", ctypes.c_int), ("res_every", ctypes.c_int), ("ref_a", ctypes.c_double),
+                ("precision", ctypes.c_int), ("refine_sweeps", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class Coeffs3(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("time", "cfl", "cpb", "cd", "cl", "cd_p", "cd_v", "cl_p", "cl_v", "nu", "cs2", "ct2")] + \
+               [("sweeps", ctypes.c_int), ("resid", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_ready = False
+
+
+def load():
+    global _ready
+    L = capi.load()
+    if not _ready:
+        D = ctypes.POINTER(ctypes.c_double)
+        V = ctypes.c_void_p
+        L.fvm3_default_params.argtypes = [ctypes.POINTER(Params3)]
+        L.fvm3_create.argtypes = [ctypes.POINTER(Params3), ctypes.POINTER(V)]
+        L.fvm3_destroy.argtypes = [V]
+        L.fvm3_last_error.argtypes = [V]
+        L.fvm3_last_error.restype = ctypes.c_char_p
+        L.fvm3_set_grid.argtypes = [V, D, D, D]
+        L.fvm3_init.argtypes = [V, D, D, D]
+        L.fvm3_step.argtypes = [V, ctypes.c_int, ctypes.POINTER(Coeffs3)]
+        L.fvm3_get_array.argtypes = [V, ctypes.c_char_p, D]
+        L.fvm3_set_array.argtypes = [V, ctypes.c_char_p, D]
+        L.fvm3_sgs.argtypes = [V, ctypes.POINTER(Coeffs3)]
+        L.fvm3_time_sweeps.argtypes = [V, ctypes.c_int, D]
+        L.fvm3_get_stream.argtypes = [V, ctypes.POINTER(V)]
+        _ready = True
+    return L
+
+
+def default_params(**kw) -> Params3:
+    p = Params3()
+    load().fvm3_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Context3:
+    """One 3-D LES solver context (one CUDA stream)."""
+
+    def __init__(self, params: Params3):
+        self.L = load()
+        self.p = params
+        self.ni, self.nj, self.nk = params.ni, params.nj, params.nk
+        self.shape = (self.nk + 1, self.nj + 1, self.ni + 1)
+        self.n = int(np.prod(self.shape))
+        h = ctypes.c_void_p()
+        rc = self.L.fvm3_create(ctypes.byref(params), ctypes.byref(h))
+        if rc != capi.FVM_OK:
+            raise capi.FvmError(rc, "fvm3_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fvm3_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc, allow=()):
+        if rc != capi.FVM_OK and rc not in allow:
+            raise capi.FvmError(rc, self.L.fvm3_last_error(self.h).decode())
+        return rc
+
+    def _arr(self, a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        if a.size != self.n:
+            raise ValueError(f"array has {a.size} elements, expected {self.n}")
+        return a
+
+    def set_grid(self, g):
+        x, y, z = self._arr(g.xg), self._arr(g.yg), self._arr(g.zg)
+        self._ok(self.L.fvm3_set_grid(self.h, _dp(x), _dp(y), _dp(z)))
+
+    def init(self, du=None, dv=None, dw=None):
+        a, b, c = self._arr(du), self._arr(dv), self._arr(dw)
+        self._ok(self.L.fvm3_init(self.h, _dp(a), _dp(b), _dp(c)))
+
+    def step(self, n=1) -> dict:
+        c = Coeffs3()
+        self._ok(self.L.fvm3_step(self.h, n, ctypes.byref(c)), allow=(capi.FVM_ERR_NOCONV,))
+        return c.as_dict()
+
+    def sgs(self) -> dict:
+        c = Coeffs3()
+        self._ok(self.L.fvm3_sgs(self.h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def get(self, name) -> np.ndarray:
+        out = np.empty(self.n)
+        self._ok(self.L.fvm3_get_array(self.h, name.encode(), _dp(out)))
+        return out.reshape(self.shape)
+
+    def set(self, name, a):
+        a = self._arr(a)
+        self._ok(self.L.fvm3_set_array(self.h, name.encode(), _dp(a)))
+
+    def time_sweeps(self, sweeps=50) -> float:
+        ms = ctypes.c_double()
+        self._ok(self.L.fvm3_time_sweeps(self.h, sweeps, ctypes.byref(ms)))
+        return ms.value
+
+    def stream_handle(self) -> int:
+        s = ctypes.c_void_p()
+        self._ok(self.L.fvm3_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0

@@ -129,3 +129,74 @@ def perturbation(ni: int, nj: int, amp: float, seed: int):
     du[1:nj, 1:ni] = amp * rng.uniform(-1.0, 1.0, size=(nj - 1, ni - 1))
     dv[1:nj, 1:ni] = amp * rng.uniform(-1.0, 1.0, size=(nj - 1, ni - 1))
     return du, dv
+
+
+class OGrid3D:
+    """Extruded O-grid: node arrays shaped (NK+1, NJ+1, NI+1), node (i,j,k) at
+    [k, j, i] for i=1..NI, j=1..NJ, k=1..NK (index 0 unused), i.e. the reference
+    storage (0:NI,0:NJ,0:NK) in Fortran order when flattened."""
+
+    def __init__(self, ni, nj, nk, xg, yg, zg, lz):
+        self.ni, self.nj, self.nk = ni, nj, nk
+        self.xg, self.yg, self.zg = xg, yg, zg
+        self.lz = lz
+
+    @property
+    def cells(self) -> int:
+        return (self.ni - 1) * (self.nj - 1) * (self.nk - 1)
+
+    @property
+    def shape(self):
+        return (self.nk + 1, self.nj + 1, self.ni + 1)
+
+
+def o_grid_3d(n_theta: int, n_r: int, n_z: int, lz: float = math.pi, r_in: float = 0.5, r_out: float = 50.0,
+              dr1: float = 0.001, skew: float = 0.0) -> OGrid3D:
+    """The 2-D O-grid law extruded over n_z spanwise cells of length lz (z of node
+    k is lz*(k-1)/n_z, as the reference's grid generator lays out the span)."""
+    g = o_grid(n_theta, n_r, r_in=r_in, r_out=r_out, dr1=dr1, skew=skew)
+    nk = n_z + 1
+    shape = (nk + 1, g.nj + 1, g.ni + 1)
+    xg, yg, zg = np.zeros(shape), np.zeros(shape), np.zeros(shape)
+    for k in range(1, nk + 1):
+        xg[k] = g.xg
+        yg[k] = g.yg
+        zg[k, 1:, 1:] = lz * (k - 1) / n_z
+    return OGrid3D(g.ni, g.nj, nk, xg, yg, zg, lz)
+
+
+def write_grid_file_3d(path: str, g: OGrid3D) -> None:
+    """The reference's NNNxMMMxKKK.dat format (grid.f90:52-66): one x y z triple
+    per record, I fastest, then J, then K."""
+    with open(path, "w") as f:
+        for k in range(1, g.nk + 1):
+            for j in range(1, g.nj + 1):
+                for i in range(1, g.ni + 1):
+                    f.write(f"{float(g.xg[k, j, i])!r} {float(g.yg[k, j, i])!r} {float(g.zg[k, j, i])!r}\n")
+
+
+def read_grid_file_3d(path: str, ni: int, nj: int, nk: int, lz: float = float("nan")) -> OGrid3D:
+    vals = np.loadtxt(path).reshape(nk, nj, ni, 3)
+    shape = (nk + 1, nj + 1, ni + 1)
+    xg, yg, zg = np.zeros(shape), np.zeros(shape), np.zeros(shape)
+    xg[1:, 1:, 1:] = vals[..., 0]
+    yg[1:, 1:, 1:] = vals[..., 1]
+    zg[1:, 1:, 1:] = vals[..., 2]
+    return OGrid3D(ni, nj, nk, xg, yg, zg, lz)
+
+
+def grid_file_name_3d(ni: int, nj: int, nk: int) -> str:
+    """'NNNxMMMxKKK.dat' (grid.f90:46-50)."""
+    return f"{ni:03d}x{nj:03d}x{nk:03d}.dat"
+
+
+def perturbation_3d(ni: int, nj: int, nk: int, amp: float, seed: int):
+    """Seeded uniform(-amp, amp) perturbations of U, V, W on the interior cells
+    (full (NK+1, NJ+1, NI+1) arrays, zero on ghost cells)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(3):
+        a = np.zeros((nk + 1, nj + 1, ni + 1))
+        a[1:nk, 1:nj, 1:ni] = amp * rng.uniform(-1.0, 1.0, size=(nk - 1, nj - 1, ni - 1))
+        out.append(a)
+    return tuple(out)

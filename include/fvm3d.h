@@ -1,0 +1,74 @@
+/*
+ * fvm3d.h -- C-ABI of the GB300 3-D LES time step of the cylinder solver: the
+ * reference's LES/v2.3_LES-Reynolds stresses/ driver (main.f90:33-147) on one GPU
+ * owning the whole domain.  The reference's MPI halo exchange (mpi_x.f90) becomes
+ * the periodic index wrap / ghost copy of a single rank.
+ *
+ * Arrays are the reference's (0:NI,0:NJ,0:NK) arrays in Fortran order, element
+ * (i,j,k) at i + (NI+1)*(j + (NJ+1)*k): I radial, J circumferential (periodic
+ * through the branch cut), K spanwise (periodic).  All entry points return an int
+ * status (FVM_OK, FVM_ERR_*, as in fvm.h) and never abort.
+ */
+#ifndef FVM3D_H
+#define FVM3D_H
+
+#include "fvm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fvm3_params {
+    int ni, nj, nk;        /* node counts (comdat_param.f90:6-8); NJ-1 and NK-1 must be even */
+    double re, pr, dt;     /* RE, PR, DTIME (comdat_param.f90:37-45) */
+    double tin, t_wall;    /* TIN, T_WALL */
+    double resimax;        /* Poisson scaled-L1 tolerance (RESIMAX) */
+    int nswpp;             /* Poisson sweep cap (NSWPP) */
+    int use_les;           /* USE_LES: dynamic Smagorinsky SGS terms */
+    int les_zavg;          /* 0: coefficient averaged over the volume (the reference's,
+                              stress_tensor_dy.f90:486-517); 1: Lilly least squares along
+                              the span per (I,J), clipped at zero */
+    int thermal;           /* advance T (ITER_T, BCT) */
+    int res_every;         /* Poisson residual every k-th sweep */
+    double ref_a;          /* reference area of the force coefficients (REF_A) */
+    int precision;         /* FVM_FP64, or FVM_MIXED: FP32 red-black Poisson sweeps on the
+                              correction inside FP64 residual refinement */
+    int refine_sweeps;     /* MIXED: FP32 sweeps per FP64 residual */
+    int device;
+} fvm3_params;
+
+typedef struct fvm3_coeffs {
+    double time, cfl, cpb, cd, cl, cd_p, cd_v, cl_p, cl_v, nu;
+    double cs2, ct2;       /* dynamic coefficients of the step (volume mode) */
+    int sweeps;
+    double resid;
+} fvm3_coeffs;
+
+struct fvm3_ctx;
+
+/* Defaults: the reference's PARAMETERs where it has them (comdat_param.f90). */
+int fvm3_default_params(fvm3_params *p);
+int fvm3_create(const fvm3_params *p, struct fvm3_ctx **ctx);
+int fvm3_destroy(struct fvm3_ctx *ctx);
+const char *fvm3_last_error(const struct fvm3_ctx *ctx);
+/* GRID + METRIC (grid.f90:46-320, metric.f90:33-520) from node coordinates and the
+ * geometry part of INIT (init.f90:150-200). */
+int fvm3_set_grid(struct fvm3_ctx *ctx, const double *xg, const double *yg, const double *zg);
+/* INIT: uniform flow, du/dv/dw (may be NULL) added to the interior. */
+int fvm3_init(struct fvm3_ctx *ctx, const double *du, const double *dv, const double *dw);
+/* nsteps time steps (main.f90:33-147); out (may be NULL): the last step's record. */
+int fvm3_step(struct fvm3_ctx *ctx, int nsteps, fvm3_coeffs *out);
+/* Named arrays ("U","V","W","P","T","NLX","NLY","NLZ","ADV","DJAC","SGS_X",...). */
+int fvm3_get_array(struct fvm3_ctx *ctx, const char *name, double *out);
+int fvm3_set_array(struct fvm3_ctx *ctx, const char *name, const double *in);
+/* One application of the SGS model (STRESS_TENSOR_DY) to the current state, for
+ * tests of the model alone. */
+int fvm3_sgs(struct fvm3_ctx *ctx, fvm3_coeffs *out);
+/* Time of `sweeps` Poisson sweeps (both colours, state unchanged). */
+int fvm3_time_sweeps(struct fvm3_ctx *ctx, int sweeps, double *ms_per_sweep);
+int fvm3_get_stream(struct fvm3_ctx *ctx, void **stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

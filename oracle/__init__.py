@@ -6,6 +6,7 @@ module, as the checker.  The product never imports it.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import subprocess
 
@@ -154,3 +155,93 @@ class Oracle:
 
     def set_time(self, t, niter=0):
         lib().orc_set_time(self._h, t, niter)
+
+
+# ---------------------------------------------------------------------------
+# 3-D LES restatement (fvm3d_oracle.c)
+# ---------------------------------------------------------------------------
+O3_FAITHFUL, O3_GPU = 0, 1
+
+
+class Params3D(ctypes.Structure):
+    _fields_ = [("ni", ctypes.c_int), ("nj", ctypes.c_int), ("nk", ctypes.c_int),
+                ("re", ctypes.c_double), ("pr", ctypes.c_double), ("dt", ctypes.c_double),
+                ("tin", ctypes.c_double), ("t_wall", ctypes.c_double), ("resimax", ctypes.c_double),
+                ("nswpp", ctypes.c_int), ("order", ctypes.c_int), ("use_les", ctypes.c_int),
+                ("les_zavg", ctypes.c_int), ("thermal", ctypes.c_int), ("res_every", ctypes.c_int),
+                ("ref_a", ctypes.c_double)]
+
+
+class Coeffs3D(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("time", "cfl", "cpb", "cd", "cl", "cd_p", "cd_v", "cl_p", "cl_v", "nu", "cs2", "ct2")] + \
+               [("sweeps", ctypes.c_int), ("resid", ctypes.c_double)]
+
+
+class Oracle3D:
+    """The 3-D LES step of the reference restated in C (test infrastructure).
+    Arrays are numpy views shaped (NK+1, NJ+1, NI+1)."""
+
+    def __init__(self, ni, nj, nk, re=3900.0, pr=0.71, dt=0.002, order=O3_GPU, resimax=1e-10, nswpp=100000,
+                 use_les=True, les_zavg=False, thermal=True, res_every=2, ref_a=None, lz=math.pi,
+                 tin=0.0, t_wall=1.0):
+        L = lib()
+        if not hasattr(L, "_o3_ready"):
+            P = ctypes.POINTER(ctypes.c_double)
+            L.o3_create.restype = ctypes.c_void_p
+            L.o3_create.argtypes = [ctypes.POINTER(Params3D)]
+            L.o3_destroy.argtypes = [ctypes.c_void_p]
+            L.o3_set_grid.argtypes = [ctypes.c_void_p, P, P, P]
+            L.o3_init.argtypes = [ctypes.c_void_p, P, P, P]
+            L.o3_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.o3_last_coeffs.restype = ctypes.POINTER(Coeffs3D)
+            L.o3_last_coeffs.argtypes = [ctypes.c_void_p]
+            L.o3_array.restype = P
+            L.o3_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+            L.o3_sgs.argtypes = [ctypes.c_void_p]
+            L._o3_ready = True
+        self.ni, self.nj, self.nk = ni, nj, nk
+        if ref_a is None:
+            ref_a = 1.0 * lz          # diameter x span
+        p = Params3D(ni=ni, nj=nj, nk=nk, re=re, pr=pr, dt=dt, tin=tin, t_wall=t_wall, resimax=resimax,
+                     nswpp=nswpp, order=order, use_les=int(use_les), les_zavg=int(les_zavg), thermal=int(thermal),
+                     res_every=res_every, ref_a=ref_a)
+        self._h = L.o3_create(ctypes.byref(p))
+        if not self._h:
+            raise MemoryError("o3_create failed")
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().o3_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def set_grid(self, g):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (g.xg, g.yg, g.zg)]
+        rc = lib().o3_set_grid(self._h, *[_dptr(a) for a in arrs])
+        if rc != 0:
+            raise ValueError(f"o3_set_grid failed ({rc})")
+
+    def init(self, du=None, dv=None, dw=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (du, dv, dw)]
+        lib().o3_init(self._h, *[None if a is None else _dptr(a) for a in arrs])
+
+    def step(self, n=1):
+        rc = lib().o3_step(self._h, n)
+        if rc != 0:
+            raise FloatingPointError(f"o3_step failed ({rc})")
+
+    def sgs(self):
+        lib().o3_sgs(self._h)
+
+    def array(self, name) -> np.ndarray:
+        p = lib().o3_array(self._h, name.encode())
+        if not p:
+            raise KeyError(name)
+        return np.ctypeslib.as_array(p, shape=(self.nk + 1, self.nj + 1, self.ni + 1))
+
+    def coeffs(self) -> dict:
+        c = lib().o3_last_coeffs(self._h).contents
+        return {n: getattr(c, n) for n, _ in Coeffs3D._fields_}
