@@ -302,7 +302,7 @@ def run_ours(args):
 # discrete adjoint: d(mean Cd over a window)/d(rotation, blowing) on the 128 x 96 grid
 # ---------------------------------------------------------------------------------
 ADJOINT = dict(name="adjoint-cylinder2d-re100-128x96", n_theta=128, n_r=96, re=100.0, pr=0.71, dt=0.005,
-               resimax=1e-10, nswpp=100000, amp=1e-3, seed=0, dr1=0.005, r_out=50.0, window=500, ckpt=50,
+               resimax=1e-10, nswpp=100000, amp=1e-3, seed=0, dr1=0.005, r_out=50.0, window=100, ckpt=10,
                omega=0.0, blow_sigma=0.01)
 
 
@@ -324,7 +324,10 @@ def adjoint_measure(spinup, precision, device, fd_check=True):
     ctx.init(du, dv)
     blow = a["blow_sigma"] * np.random.default_rng(a["seed"]).standard_normal(g.nj - 1)
     ctx.set_controls(a["omega"], blow)
+    t0 = time.perf_counter()
     ctx.step(spinup)
+    torch.cuda.synchronize()
+    print(f"adjoint workload: spin-up {spinup} steps {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
     start = {nm: ctx.get(nm) for nm in ("U", "V", "P", "T", "NLX", "NLY", "ADV")}
 
     def restore():
@@ -347,6 +350,7 @@ def adjoint_measure(spinup, precision, device, fd_check=True):
     J, dw, db = ctx.adjoint_drag_grad(a["window"], a["ckpt"])
     torch.cuda.synchronize()
     t_adj = time.perf_counter() - t0
+    print(f"adjoint workload: window forward {t_fwd:.2f} s, adjoint {t_adj:.2f} s", file=sys.stderr, flush=True)
     out = {"J": J, "dJ_domega": dw, "dJ_dblow_norm": float(np.linalg.norm(db)), "forward_s": t_fwd,
            "adjoint_s": t_adj, "adjoint_over_forward": t_adj / t_fwd, "J_vs_forward": abs(J - j_fwd) / abs(j_fwd),
            "spinup_steps": spinup}
@@ -543,7 +547,7 @@ def main():
     ap.add_argument("--workload", choices=["cylinder2d", "sweep64", "adjoint"], default="cylinder2d",
                     help="sweep64: 64 ragged cases advanced as batches, sharded over the ranks; "
                          "adjoint: window-drag gradient on the 128x96 grid")
-    ap.add_argument("--spinup", type=int, default=2000, help="adjoint workload: steps before the window")
+    ap.add_argument("--spinup", type=int, default=200, help="adjoint workload: steps before the window")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

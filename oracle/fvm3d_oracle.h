@@ -4,6 +4,12 @@
  * infrastructure: the 3-D parity tests call it as the checker.  The product never
  * links or calls this code.
  *
+ * Pinned: in O3_FAITHFUL order it reproduces, to rounding (fields <= 1e-12
+ * relative L2, coefficient records <= 1e-11), the golden fixtures made by
+ * executing the reference's own Fortran sources of this solver
+ * (tests/golden/make_golden.py, cases les3d_* and dns3d_*: LES and no-LES steps
+ * on skewed and circular grids at the reference's Poisson settings).
+ *
  * One process owns the whole domain.  The reference's halo exchange MPI_X
  * (mpi_x.f90) with a single periodic rank is a periodic copy: J=0 <- NJ-1,
  * J=NJ <- 1 (for every K), then K=0 <- NK-1, K=NK <- 1 (for every J).  Sums and

@@ -80,7 +80,7 @@ def logical_lines(text: str):
 # expression parsing
 # ---------------------------------------------------------------------------------
 TOKEN = re.compile(r"""
-    (?P<num>(\d+\.\d*|\.\d+|\d+)([dDeE][+-]?\d+)?)
+    (?P<num>(\d+\.(?!(and|or|not|eq|ne|lt|le|gt|ge|true|false)\.)\d*|\.\d+|\d+)([dDeE][+-]?\d+)?)
   | (?P<dot>\.(and|or|not|eq|ne|lt|le|gt|ge|true|false)\.)
   | (?P<str>'[^']*'|"[^"]*")
   | (?P<name>[A-Za-z_][A-Za-z0-9_]*)
@@ -318,6 +318,9 @@ def binop(op, a, b):
         if isinstance(a, (int, np.integer)) and isinstance(b, (int, np.integer)):
             q = abs(int(a)) // abs(int(b))
             return q if (a >= 0) == (b >= 0) else -q
+        if not isinstance(a, np.ndarray) and not isinstance(b, np.ndarray) and b == 0:
+            with np.errstate(divide="ignore", invalid="ignore"):   # IEEE: inf or NaN, as compiled code
+                return float(np.float64(a) / np.float64(b))
         return a / b
     raise ValueError(op)
 
@@ -374,6 +377,7 @@ class Machine:
         self.unit_in = {}      # unit -> list of values
         self.unit_out = {}     # unit -> list of records
         self.units_open = {}
+        self.g.update(MPI_CONSTANTS)
 
     # -- declarations -----------------------------------------------------------
     def declare(self, st, scope, types, env):
@@ -538,7 +542,13 @@ def split_top(s: str):
 # statement compilation
 # ---------------------------------------------------------------------------------
 DECL = re.compile(r"^(INTEGER|DOUBLE\s+PRECISION|LOGICAL|CHARACTER)\b", re.I)
-IGNORE = re.compile(r"^(IMPLICIT|SAVE|USE|PRINT|FORMAT|CLOSE|PAUSE|DEALLOCATE)\b", re.I)
+IGNORE = re.compile(r"^(IMPLICIT|SAVE|USE|PRINT|FORMAT|CLOSE|PAUSE|DEALLOCATE|INCLUDE|CONTINUE)\b", re.I)
+
+# MPI for a single rank with periodic Cartesian neighbours: every neighbour is the
+# rank itself, SENDRECV copies the send buffer into the receive buffer, ALLREDUCE
+# copies its argument.  Handle and datatype constants are plain integers.
+MPI_CONSTANTS = {"MPI_DOUBLE_PRECISION": 1, "MPI_SUM": 1, "MPI_MAX": 2, "MPI_MIN": 3, "MPI_COMM_WORLD": 0,
+                 "MPI_STATUS_SIZE": 6, "MPI_INTEGER": 2}
 
 
 def parse_block(lines, i, enders):
@@ -808,6 +818,25 @@ def exec_stmt(M, s, env):
 def call(M, name, args, env):
     if name == "CPU_TIME":
         M.assign(args[0], 0.0, env)
+        return
+    if name.startswith("MPI_") and name not in M.subs:
+        if name in ("MPI_COMM_RANK",):
+            M.assign(args[1], 0, env)
+        elif name == "MPI_COMM_SIZE":
+            M.assign(args[1], 1, env)
+        elif name == "MPI_CART_CREATE":
+            M.assign(args[5], 0, env)
+        elif name == "MPI_CART_COORDS":
+            arr = M.eval(args[3], env)
+            M.assign(args[3], np.zeros_like(np.asarray(arr)) if isinstance(arr, np.ndarray) else 0, env)
+        elif name == "MPI_CART_SHIFT":
+            M.assign(args[3], 0, env)
+            M.assign(args[4], 0, env)
+        elif name == "MPI_SENDRECV":
+            val = M.eval(args[0], env)
+            M.assign(args[5], np.array(val, copy=True) if isinstance(val, np.ndarray) else val, env)
+        elif name == "MPI_ALLREDUCE":
+            M.assign(args[1], M.eval(args[0], env), env)
         return
     r = M.subs[name]
     local = M.saved.setdefault(name, {"__types__": {}})

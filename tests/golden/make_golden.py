@@ -1,7 +1,7 @@
 """Generate the golden fixtures by running the reference's own Fortran sources.
 
 Usage (only where the reference tree exists):
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py /root/reference [--3d-only]
 
 For each case the R2D snapshot (cylinder/cylinder_v3.0.3_AF_original 4step_face_nl)
 is executed by ftn_interp with NI, NJ (and where stated NSWPP, RESIMAX) replaced in
@@ -11,6 +11,16 @@ fed in.  Main's statements up to CALL INIT run once, then the statements between
 label 777 and the time-loop test run once per step.  Saved: U, V, P, T and the
 NLX/NLY/ADV history after the last step, and every record CALCCOEF appends to
 NU_CD_CL.PLT (time, Nu, Cd, Cl, Cpb, Cd_p, Cd_v, Cl_p, Cl_v, CFL).
+
+The 3-D cases run the LES solver (LES/v2.3_LES-Reynolds stresses) the same way on
+one rank (NDIMJ = NDIMK = 1; the MPI calls are served by ftn_interp's one-rank
+stubs): GRID reads the node triples of fvm_gb300.grid.o_grid_3d from unit 10, the
+seeded perturbation_3d is added to U, V, W after INIT, and the statements of the
+time loop run once per step.  Saved: U, V, W, P, T, NLX, NLY, NLZ, ADV in
+(NK+1, NJ+1, NI+1) order and the CALCCOEF records.  With USE_LES = 0 the
+reference still writes YPLUS in CALCCOEF although INIT allocates it only for LES
+(calccoef.f90:121, init.f90:79-81); the harness allocates it so that the run
+proceeds (YPLUS is written, never read, on the path).
 """
 from __future__ import annotations
 
@@ -48,6 +58,62 @@ CASES = [
 ]
 
 
+SNAPSHOT3D = os.path.join("LES", "v2.3_LES-Reynolds stresses")
+FILES3D = ["comdat_param.f90", "comdat_shared.f90", "define.f90", "mpi_x.f90", "grid.f90", "metric.f90", "init.f90",
+           "contra_vel.f90", "nl.f90", "dif.f90", "dif_diagonal.f90", "p_source.f90", "iter_u.f90", "iter_p.f90",
+           "lisolv.f90", "bcu.f90", "bcp.f90", "bct.f90", "iter_t.f90", "test_filter.f90", "stress_tensor_dy.f90",
+           "calccoef.f90", "main.f90"]
+FIELDS3D = ["U", "V", "W", "P", "T", "NLX", "NLY", "NLZ", "ADV"]
+
+CASES3D = [
+    # the reference's own settings (LES on, NSWPP=20, RESIMAX=1e-4) on a skewed grid
+    dict(name="les3d_12x8x6_re3900", n_theta=12, n_r=8, n_z=6, skew=0.2, re=3900.0, pr=0.71, dt=0.002, amp=0.05,
+         seed=1, steps=3, use_les=1, over={}),
+    # stronger skew, lower Reynolds number, unit Prandtl number
+    dict(name="les3d_16x12x8_re1000_skew", n_theta=16, n_r=12, n_z=8, skew=0.3, re=1000.0, pr=1.0, dt=0.003,
+         amp=0.05, seed=3, steps=2, use_les=1, over={}),
+    # no SGS model, circular section
+    dict(name="dns3d_12x8x6_re300_polar", n_theta=12, n_r=8, n_z=6, skew=0.0, re=300.0, pr=0.71, dt=0.004,
+         amp=0.05, seed=2, steps=2, use_les=0, over={}),
+]
+
+
+def run_case_3d(ref_root, c):
+    import math
+    from fvm_gb300.grid import o_grid_3d, perturbation_3d
+    g = o_grid_3d(c["n_theta"], c["n_r"], c["n_z"], lz=math.pi, dr1=0.01, skew=c["skew"])
+    over = {"NI": g.ni, "NJ": g.nj, "NK": g.nk, "NDIMJ": 1, "NDIMK": 1, "RE": c["re"], "PR": c["pr"],
+            "PE": c["re"] * c["pr"], "DTIME": c["dt"], "USE_LES": c["use_les"]}
+    over.update(c["over"])
+    M = F.load_program(os.path.join(ref_root, SNAPSHOT3D), FILES3D, over)
+    vals = []
+    for k in range(1, g.nk + 1):          # grid.f90: one (x, y, z) record per node, I fastest
+        for j in range(1, g.nj + 1):
+            for i in range(1, g.ni + 1):
+                vals += [float(g.xg[k, j, i]), float(g.yg[k, j, i]), float(g.zg[k, j, i])]
+    M.unit_in[10] = vals
+    main = M.subs["__MAIN__"].body
+    k_init = next(k for k, s in enumerate(main) if s[0] == "call" and s[2] == "INIT")
+    F.run_stmts(M, main[:k_init + 1], None)
+    if M.g.get("YPLUS") is None:
+        M.g["YPLUS"] = F.FArray([1, 1, 1], [1, g.nj - 1, g.nk - 1])
+    du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, c["amp"], c["seed"])
+    for nm, dd in (("U", du), ("V", dv), ("W", dw)):
+        M.g[nm].a[...] += dd.transpose(2, 1, 0)
+    k777 = next(k for k, s in enumerate(main) if s[1] == 777)
+    kend = next(k for k, s in enumerate(main) if s[0] == "lif" and s[3] and s[3][0][0] == "goto")
+    # the loop body without the output routines this restatement does not cover
+    keep = set(M.subs)
+    step = [s for s in main[k777:kend] if not (s[0] == "call" and s[2] not in keep and not s[2].startswith("MPI_"))]
+    step[0] = ("assign", None) + step[0][2:] if step[0][0] == "assign" else ("nop", None)
+    for _ in range(c["steps"]):
+        F.run_stmts(M, step, None)
+    out = {nm: M.g[nm].a.transpose(2, 1, 0).copy() for nm in FIELDS3D}
+    recs = [r for r in M.unit_out.get(11, []) if r and not isinstance(r[0], str)]
+    out["COEFFS"] = np.array(recs, dtype=np.float64)
+    return g, out
+
+
 def run_case(ref_root, c):
     g = o_grid(c["n_theta"], c["n_r"], skew=c["skew"])
     over = {"NI": g.ni, "NJ": g.nj}
@@ -75,9 +141,14 @@ def run_case(ref_root, c):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    pos = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref_root = pos[0] if pos else "/root/reference"
+    only3d = "--3d-only" in sys.argv
     manifest = []
-    for c in CASES:
+    if only3d:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest = json.load(f)["cases"]
+    for c in ([] if only3d else CASES):
         t0 = time.time()
         g, out = run_case(ref_root, c)
         fn = f"{c['name']}.npz"
@@ -88,9 +159,21 @@ def main():
                              resimax=float(c["over"].get("RESIMAX", 1e-4)), amp=0.0, seed=0,
                              fields=["U", "V", "P", "T", "NLX", "NLY", "ADV"], order=0, tol=1e-12))
         print(f"{c['name']}: {time.time() - t0:.1f} s, {len(out['COEFFS'])} coefficient records", flush=True)
+    manifest3d = []
+    for c in CASES3D:
+        t0 = time.time()
+        g, out = run_case_3d(ref_root, c)
+        fn = f"{c['name']}.npz"
+        np.savez_compressed(os.path.join(HERE, fn), **out)
+        manifest3d.append(dict(name=c["name"], file=fn, n_theta=c["n_theta"], n_r=c["n_r"], n_z=c["n_z"],
+                               skew=c["skew"], dr1=0.01, lz="pi", re=c["re"], pr=c["pr"], dt=c["dt"],
+                               steps=c["steps"], nswpp=int(c["over"].get("NSWPP", 20)),
+                               resimax=float(c["over"].get("RESIMAX", 1e-4)), amp=c["amp"], seed=c["seed"],
+                               use_les=c["use_les"], ref_a=6.283185307, fields=FIELDS3D, tol=1e-12))
+        print(f"{c['name']}: {time.time() - t0:.1f} s, {len(out['COEFFS'])} coefficient records", flush=True)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py (reference sources executed by ftn_interp)",
-                   "cases": manifest}, f, indent=1)
+                   "cases": manifest, "cases3d": manifest3d}, f, indent=1)
 
 
 if __name__ == "__main__":
