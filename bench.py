@@ -385,6 +385,196 @@ def run_adjoint_bench(args):
 
 
 # ---------------------------------------------------------------------------------
+# 3-D LES (include/fvm3d.h) on the 256 theta x 192 r x 48 z O-grid, FP64 and mixed
+# ---------------------------------------------------------------------------------
+LES3D = dict(name="les3d-re3900-256x192x48", n_theta=256, n_r=192, n_z=48, re=3900.0, pr=0.71, dt=0.002,
+             dr1=0.001, amp=0.05, seed=0, resimax=1e-8, nswpp=3000, res_every=4, refine_sweeps=16, zavg=1,
+             thermal=1)
+FIELDS3D = ("U", "V", "W", "P", "T", "NLX", "NLY", "NLZ", "ADV")
+
+
+def les3d_inputs(w):
+    import math
+    from fvm_gb300.grid import o_grid_3d, perturbation_3d
+    g = o_grid_3d(w["n_theta"], w["n_r"], w["n_z"], lz=math.pi, dr1=w["dr1"])
+    du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, w["amp"], w["seed"])
+    return g, du, dv, dw
+
+
+def make_ctx3(w, precision, device, g, du, dv, dw):
+    from fvm_gb300 import capi3d
+    p = capi3d.default_params(ni=g.ni, nj=g.nj, nk=g.nk, re=w["re"], pr=w["pr"], dt=w["dt"], resimax=w["resimax"],
+                              nswpp=w["nswpp"], use_les=1, les_zavg=w["zavg"], thermal=w["thermal"],
+                              res_every=w["res_every"], refine_sweeps=w["refine_sweeps"], precision=precision,
+                              ref_a=float(g.zg[g.nk, 1, 1] - g.zg[1, 1, 1]), device=device)
+    ctx = capi3d.Context3(p)
+    ctx.set_grid(g)
+    ctx.init(du, dv, dw)
+    return ctx
+
+
+def roofline_sweep3d(n_int, ms_per_launch, peaks, mixed):
+    """Roofline of the 3-D Poisson line kernel from its average launch time (one
+    colour = half the I lines).  Algorithmic bytes per active cell:
+    FP32 (k3_line32): RF, ANf, ASf, ATf, ABf, invDf, faf, fbf read, DF written, the
+    other colour's DF read once: 40 B.  FP64 (k3_line): SU, AN, AS, AT, AB, invD,
+    fa, fb read, P written, the other colour's P read once: 80 B."""
+    if not ms_per_launch or ms_per_launch <= 0:
+        return None
+    per_launch = (40.0 if mixed else 80.0) * (n_int // 2)
+    achieved = per_launch / (ms_per_launch * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs") if peaks else None
+    src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "k3_line32" if mixed else "k3_line<fam 0>",
+            "avg_launch_us": ms_per_launch * 1e3, "bytes_per_launch": per_launch, "peak_source": src}
+
+
+def cpu_baseline_3d(w, g, du, dv, dw, sweeps_gpu):
+    """Serial CPU restatement (reference order) on a bounded sample: one step with
+    the Poisson capped at 20 sweeps and one capped at 120 give the fixed cost of a
+    step and the cost of one sweep; the rate is extrapolated to the GPU run's
+    sweeps per step and labelled as such."""
+    import oracle
+    t = {}
+    for cap in (20, 120):
+        o = oracle.Oracle3D(g.ni, g.nj, g.nk, re=w["re"], pr=w["pr"], dt=w["dt"], order=oracle.O3_FAITHFUL,
+                            resimax=w["resimax"], nswpp=cap, use_les=True, les_zavg=bool(w["zavg"]),
+                            thermal=bool(w["thermal"]), ref_a=float(g.zg[g.nk, 1, 1] - g.zg[1, 1, 1]))
+        o.set_grid(g)
+        o.init(du, dv, dw)
+        t0 = time.perf_counter()
+        o.step(1)
+        t[cap] = time.perf_counter() - t0
+        del o
+    per_sweep = max((t[120] - t[20]) / 100.0, 0.0)
+    fixed = max(t[20] - 20 * per_sweep, 0.0)
+    est = fixed + per_sweep * sweeps_gpu
+    n_int = (g.ni - 1) * (g.nj - 1) * (g.nk - 1)
+    return {"value": n_int / est / 1e6, "unit": "Mcell-steps/s", "cores": 1, "kind": "port",
+            "sample": f"first step twice, Poisson capped at 20 and 120 sweeps ({t[20]:.1f} s, {t[120]:.1f} s): "
+                      f"{fixed:.2f} s fixed + {per_sweep * 1e3:.1f} ms per sweep, extrapolated to "
+                      f"{sweeps_gpu} sweeps per step; serial restatement in the reference's order"}
+
+
+def run_les3d_bench(args):
+    import numpy as np
+    import torch
+    from fvm_gb300 import capi, dist
+
+    rank, world = dist.init("nccl")
+    local = dist.rank_world()[2]
+    torch.cuda.set_device(local)
+    w = dict(LES3D)
+    g, du, dv, dw = les3d_inputs(w)
+    n_int = (g.ni - 1) * (g.nj - 1) * (g.nk - 1)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    res = {}
+    for name, prec in (("mixed", capi.MIXED), ("fp64", capi.FP64)):
+        ctx = make_ctx3(w, prec, local, g, du, dv, dw)
+        ext = torch.cuda.ExternalStream(ctx.stream_handle())
+        t0 = time.perf_counter()
+        ctx.step(args.warmup)
+        print(f"les3d {name}: {args.warmup} warm-up steps {time.perf_counter() - t0:.1f} s", file=sys.stderr,
+              flush=True)
+        dist.barrier()
+        clk = ClockSampler(local) if name == "mixed" else None
+        if clk:
+            clk.start()
+        ms, sweeps = 0.0, []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(ext)
+            c = ctx.step(1)
+            b.record(ext)
+            b.synchronize()
+            ms += a.elapsed_time(b)
+            sweeps.append(c["sweeps"])
+        clocks = clk.stop() if clk else None
+        dist.barrier()
+        ms = dist.max_over_ranks(ms, device="cuda")
+        sweep_ms = ctx.time_sweeps(50)
+        fields = {nm: ctx.get(nm) for nm in ("U", "V", "W", "P", "T")}
+        res[name] = dict(ms=ms, sweeps=sweeps, clocks=clocks, cd=c["cd"], resid=c["resid"], sweep_ms=sweep_ms,
+                         fields=fields)
+        print(f"les3d {name}: {ms / args.steps:.1f} ms/step, sweeps {sweeps}, sweep pair {sweep_ms * 1e3:.1f} us",
+              file=sys.stderr, flush=True)
+        ctx.close()
+    # e2e through the C-ABI with pinned host buffers (mixed path)
+    ctx = make_ctx3(w, capi.MIXED, local, g, du, dv, dw)
+    ext = torch.cuda.ExternalStream(ctx.stream_handle())
+    ctx.step(args.warmup)
+    host = {nm: torch.empty(ctx.shape, dtype=torch.float64, pin_memory=True).numpy() for nm in FIELDS3D}
+    for nm in FIELDS3D:
+        host[nm][...] = ctx.get(nm)
+    e2e_ms = 0.0
+    dist.barrier()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(ext)
+        for nm in FIELDS3D:
+            ctx.set(nm, host[nm])
+        ctx.step(1)
+        for nm in FIELDS3D:
+            host[nm][...] = ctx.get(nm)
+        b.record(ext)
+        b.synchronize()
+        e2e_ms += a.elapsed_time(b)
+    dist.barrier()
+    e2e_ms = dist.max_over_ranks(e2e_ms, device="cuda")
+    ctx.close()
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    units = world * n_int * args.steps
+    value = units / (res["mixed"]["ms"] * 1e-3) / 1e6
+    fp64_value = units / (res["fp64"]["ms"] * 1e-3) / 1e6
+    nbytes = (g.ni + 1) * (g.nj + 1) * (g.nk + 1) * 8
+    out = {
+        "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["mixed"]["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": w["name"], "grid": f"{w['n_theta']} theta x {w['n_r']} r x {w['n_z']} z cells",
+                   "cells": n_int, "re": w["re"], "dt": w["dt"], "lz": "pi", "dr1": w["dr1"],
+                   "les": "dynamic Smagorinsky, Lilly least squares along z clipped >= 0",
+                   "poisson": f"red-black I-line GS to scaled-L1 {w['resimax']:g}, cap NSWPP={w['nswpp']}",
+                   "sweeps_per_step": res["mixed"]["sweeps"],
+                   "precision": f"mixed: FP32 red-black Poisson sweeps in FP64 refinement every "
+                                f"{w['refine_sweeps']} sweeps; predictor, SGS, state FP64",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "256 MiB buffer written between timed steps (outside the events)"},
+        "fp64": {"value": fp64_value, "ms_per_step": res["fp64"]["ms"] / args.steps,
+                 "sweeps_per_step": res["fp64"]["sweeps"],
+                 "roofline": roofline_sweep3d(n_int, res["fp64"]["sweep_ms"] / 2, peaks, False)},
+        "mixed_vs_fp64": {"speedup": value / fp64_value,
+                          "field_rel_l2": {nm: rel(res["mixed"]["fields"][nm], res["fp64"]["fields"][nm])
+                                           for nm in ("U", "V", "W", "P", "T")},
+                          "cd_rel": abs(res["mixed"]["cd"] - res["fp64"]["cd"]) / abs(res["fp64"]["cd"])},
+        "roofline": roofline_sweep3d(n_int, res["mixed"]["sweep_ms"] / 2, peaks, True),
+        "e2e": {"value": units / (e2e_ms * 1e-3) / 1e6, "unit": "Mcell-steps/s",
+                "h2d_bytes_per_step": len(FIELDS3D) * nbytes, "d2h_bytes_per_step": len(FIELDS3D) * nbytes},
+        "clocks": res["mixed"]["clocks"],
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_3d(w, g, du, dv, dw, int(np.mean(res["fp64"]["sweeps"])))
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    dist.finalize()
+
+
+# ---------------------------------------------------------------------------------
 # sweep of 64 ragged cases (fvm_batch_*), sharded over the ranks by estimated cost
 # ---------------------------------------------------------------------------------
 SWEEP = dict(name="sweep64-ragged-mixed", n=64, seed=0, resimax=1e-10, nswpp=2048, refine_sweeps=32)
@@ -544,9 +734,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--parts", choices=["all", "mixed"], default="all",
                     help="'mixed' times only the headline path (for profiler runs)")
-    ap.add_argument("--workload", choices=["cylinder2d", "sweep64", "adjoint"], default="cylinder2d",
+    ap.add_argument("--workload", choices=["cylinder2d", "sweep64", "adjoint", "les3d"], default="cylinder2d",
                     help="sweep64: 64 ragged cases advanced as batches, sharded over the ranks; "
-                         "adjoint: window-drag gradient on the 128x96 grid")
+                         "adjoint: window-drag gradient on the 128x96 grid; "
+                         "les3d: 3-D LES on the 256x192x48 grid, FP64 and mixed")
     ap.add_argument("--spinup", type=int, default=200, help="adjoint workload: steps before the window")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -557,6 +748,8 @@ def main():
         run_sweep_bench(args)
     elif args.workload == "adjoint":
         run_adjoint_bench(args)
+    elif args.workload == "les3d":
+        run_les3d_bench(args)
     else:
         run_ours(args)
 

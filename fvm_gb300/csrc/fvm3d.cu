@@ -39,7 +39,7 @@ struct Coef3 {
 struct D3 {
     int NI, NJ, NK, NI1, NJ1, n, nblk;
     double re, pe, dt, rdt, tin, t_wall, pi, resimax, ref_a;
-    int nswpp, res_every, les_zavg, thermal;
+    int nswpp, res_every, les_zavg, thermal, refine_sweeps;
     // geometry
     double *XG, *YG, *ZG, *X, *Y, *Z;
     double *XIX, *XIY, *XIZ, *ETX, *ETY, *ETZ, *ZTX, *ZTY, *ZTZ, *DJAC;
@@ -57,6 +57,9 @@ struct D3 {
     // coefficient sets: [0..2] velocity splits, [3..5] temperature splits, [6] Poisson
     Coef3 cf[7];
     LineSys sys[7];
+    // MIXED Poisson: FP32 residual and correction, FP32 copies of the transverse
+    // couplings of the Poisson set
+    float *RF, *DF, *ANf, *ASf, *ATf, *ABf;
     // reductions
     PCtl *pctl;
     double *partial;        // 4 per block
@@ -893,6 +896,107 @@ __global__ void k3_pshift(D3 d)
     d.P[c] = d.P[c] - d.scal[2];
 }
 
+// ---------------------------------------------------------------------------------
+// MIXED Poisson: FP64 defect correction around FP32 red-black I-line sweeps.  Each
+// outer iteration forms in FP64 the full residual r = SU - A P, with the cross
+// term of SU recomputed from the current P (iter_p.f90:37-63, dif_diagonal.f90:
+// 13-32), its scaled-L1 norm (the convergence test of iter_p.f90:43-63) and r in
+// FP32; refine_sweeps FP32 sweeps then solve A7 dP = r from dP = 0 with the FP32
+// line factors, and P += dP in FP64 with the BCP ghosts and the periodic copy
+// refreshed.  The fixed point is the one of the FP64 iteration.
+// ---------------------------------------------------------------------------------
+__global__ void k3_coef_f32(D3 d)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    const Coef3 &cf = d.cf[6];
+    d.ANf[c] = (float)cf.AN[c];
+    d.ASf[c] = (float)cf.AS[c];
+    d.ATf[c] = (float)cf.AT[c];
+    d.ABf[c] = (float)cf.AB[c];
+}
+
+__global__ void __launch_bounds__(256) k3_mres(D3 d)
+{
+    __shared__ double sh[3 * 8];
+    __shared__ bool last;
+    if (d.pctl->done) return;
+    const int it = d.pctl->niter;
+    const Coef3 &cf = d.cf[6];
+    const int ni1 = d.NI - 1, nj1 = d.NJ - 1, total = ni1 * nj1 * (d.NK - 1);
+    double ra = 0.0, pa = 0.0, dummy = 0.0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int i = e % ni1 + 1, j = (e / ni1) % nj1 + 1, k = e / (ni1 * nj1) + 1, c = ID3(i, j, k);
+        const double *P = d.P;
+        const double su = d.DIVDT[c] - cross12(d, P, i, j, k);
+        const double r = ((((((cf.AE[c] * P[ID3(i + 1, j, k)] + cf.AW[c] * P[ID3(i - 1, j, k)]) +
+                              cf.AN[c] * P[ID3(i, jw(d, j + 1), k)]) + cf.AS[c] * P[ID3(i, jw(d, j - 1), k)]) +
+                            cf.AT[c] * P[ID3(i, j, kw(d, k + 1))]) + cf.AB[c] * P[ID3(i, j, kw(d, k - 1))]) + su) -
+                         cf.AP[c] * P[c];
+        ra += fabs(r);
+        pa += fabs(cf.AP[c] * P[c]);
+        d.RF[c] = (float)r;
+        d.DF[c] = 0.0f;
+    }
+    if (!grid_sum3(d, ra, pa, dummy, sh, last, &d.pctl->ticket)) return;
+    if (threadIdx.x == 0) {
+        const double resip = ra / pa;
+        d.pctl->resip = resip;
+        if (it > 0 && !(resip > d.resimax && it < d.nswpp)) {
+            d.pctl->done = 1;
+            d.pctl->capped = resip > d.resimax ? 1 : 0;
+        } else {
+            d.pctl->niter = it + d.refine_sweeps;
+        }
+    }
+}
+
+// One colour of the FP32 correction sweep on the I lines of the Poisson set.
+template <int M, int NW>
+__global__ void __launch_bounds__(128) k3_line32(D3 d, LineSys s, int colour, int check_done)
+{
+    constexpr int TG = WARP * NW, G = 4 / NW;
+    __shared__ float sm[G][TG * M + M * NW + 1];
+    __shared__ float xch[G][2 * NW];
+    if (check_done && d.pctl->done) return;
+    int gl, t, gib;
+    fvm::group_of<NW>(gl, t, gib);
+    int L = 0;
+    const bool active = colour_line(d, 0, colour, gl, L);
+    if (!active) L = 0;
+    const int n = s.n, j = L % (d.NJ - 1) + 1, k = L / (d.NJ - 1) + 1;
+    const int jn = jw(d, j + 1), js = jw(d, j - 1), kt = kw(d, k + 1), kb = kw(d, k - 1);
+    const float *DF = d.DF;
+    float v[M];
+#pragma unroll
+    for (int q = 0; q < M; q++) {
+        const int e = q * TG + t;
+        v[q] = 0.0f;
+        if (active && e < n) {
+            const int i = e + 1, c = ID3(i, j, k);
+            v[q] = ((d.ANf[c] * DF[ID3(i, jn, k)] + d.ASf[c] * DF[ID3(i, js, k)]) +
+                    (d.ATf[c] * DF[ID3(i, j, kt)] + d.ABf[c] * DF[ID3(i, j, kb)])) + d.RF[c];
+        }
+    }
+    fvm::to_chunks<float, M, NW>(v, sm[gib], t);
+    const size_t base = size_t(L) * TG * M;
+    fvm::group_apply<float, M, NW>(v, s.invDf + base, s.faf + base, s.fbf + base, t, xch[gib]);
+    fvm::to_interleaved<float, M, NW>(v, sm[gib], t);
+#pragma unroll
+    for (int q = 0; q < M; q++) {
+        const int e = q * TG + t;
+        if (active && e < n) d.DF[ID3(e + 1, j, k)] = v[q];
+    }
+}
+
+__global__ void k3_apply(D3 d)
+{
+    CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
+    if (d.pctl->done) return;
+    const int c = ID3(i, j, k);
+    d.P[c] = d.P[c] + (double)d.DF[c];
+}
+
 }  // namespace f3
 
 namespace f3 {
@@ -1374,6 +1478,8 @@ void carve(Bump &b, fvm3_ctx *c)
             ls.sinvf = reinterpret_cast<float *>(b.take(F.lines));
         }
     }
+    float **f32[] = {&d.RF, &d.DF, &d.ANf, &d.ASf, &d.ATf, &d.ABf};
+    for (auto p : f32) *p = reinterpret_cast<float *>(b.take((n + 1) / 2));
     d.nblk = 2 * 152;
     d.partial = b.take(4 * size_t(d.nblk));
     d.pctl = reinterpret_cast<PCtl *>(b.take(8));
@@ -1421,6 +1527,24 @@ int line(fvm3_ctx *c, int set, const double *SU, double *phi, int colour, const 
     return FVM_OK;
 }
 
+int line32(fvm3_ctx *c, int colour, int check_done)
+{
+    const D3 &d = c->d;
+    const LineSys &s = d.sys[6];
+    const int per = (c->NJ - 1) / 2 * (c->NK - 1);
+    const int blocks = fvm::line_blocks(per, s.NW);
+    bool ok = fvm::dispatch_line(s, [&](auto m, auto nw) {
+        constexpr int M = decltype(m)::value, NW = decltype(nw)::value;
+        k3_line32<M, NW><<<blocks, 128, 0, c->stream>>>(d, s, colour, check_done);
+    });
+    if (!ok) {
+        c->err = "line length above 512 cells is not supported";
+        return FVM_ERR_ARG;
+    }
+    F3CHECK(c);
+    return FVM_OK;
+}
+
 int setup_grid(fvm3_ctx *c)
 {
     D3 &d = c->d;
@@ -1443,6 +1567,7 @@ int setup_grid(fvm3_ctx *c)
         k3_coef_af<<<g_int(c), 128, 0, st>>>(d, d.cf[3 + s], s, d.pe);
     }
     k3_coef_p<<<g_int(c), 128, 0, st>>>(d, d.cf[6]);
+    k3_coef_f32<<<g_lin(c), 256, 0, st>>>(d);
     F3CHECK(c);
     for (int s = 0; s < 7; s++) {
         const int fam = s == 6 ? 0 : s % 3;
@@ -1499,11 +1624,23 @@ int poisson_graph(fvm3_ctx *c)
 {
     if (c->pgraph) return FVM_OK;
     D3 &d = c->d;
-    const int per = d.res_every, groups = std::max(1, 32 / per);
+    const bool mixed = c->p.precision == FVM_MIXED;
+    const int per = mixed ? d.refine_sweeps : d.res_every, groups = std::max(1, 32 / per);
     cudaGraph_t g = nullptr;
     F3CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int rc = FVM_OK;
-    for (int q = 0; q < groups && rc == FVM_OK; q++) {
+    for (int q = 0; q < groups && rc == FVM_OK && mixed; q++) {
+        // residual (ends the loop), FP32 correction sweeps, P += dP, ghosts
+        k3_mres<<<d.nblk, 256, 0, c->stream>>>(d);
+        for (int it = 0; it < per && rc == FVM_OK; it++) {
+            rc = line32(c, 0, 1);
+            if (rc == FVM_OK) rc = line32(c, 1, 1);
+        }
+        k3_apply<<<g_int(c), 128, 0, c->stream>>>(d);
+        k3_bcp<<<dim3((c->NJ + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, 1);
+        if (rc == FVM_OK) rc = halo(c, {d.P});
+    }
+    for (int q = 0; q < groups && rc == FVM_OK && !mixed; q++) {
         for (int it = 0; it < per && rc == FVM_OK; it++) {
             k3_psu<<<g_int(c), 128, 0, c->stream>>>(d);
             k3_bcp<<<dim3((c->NJ + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, 1);
@@ -1708,7 +1845,8 @@ int fvm3_create(const fvm3_params *p, fvm3_ctx **out)
     if ((p->nj - 1) % 2 || (p->nk - 1) % 2) return FVM_ERR_ARG;
     if (p->ni - 1 > 512 || p->nj - 1 > 512 || p->nk - 1 > 512) return FVM_ERR_ARG;
     if (!(p->dt > 0.0) || !(p->re > 0.0) || !(p->pr > 0.0) || p->nswpp < 1 || !(p->ref_a > 0.0)) return FVM_ERR_ARG;
-    if (p->precision != FVM_FP64) return FVM_ERR_ARG;
+    if (p->precision != FVM_FP64 && p->precision != FVM_MIXED) return FVM_ERR_ARG;
+    if (p->precision == FVM_MIXED && p->refine_sweeps < 1) return FVM_ERR_ARG;
     fvm3_ctx *c = new (std::nothrow) fvm3_ctx();
     if (!c) return FVM_ERR_NOMEM;
     c->p = *p;
@@ -1723,6 +1861,9 @@ int fvm3_create(const fvm3_params *p, fvm3_ctx **out)
     d.res_every = p->res_every < 1 ? 1 : p->res_every;
     d.nswpp = ((p->nswpp + d.res_every - 1) / d.res_every) * d.res_every;
     d.les_zavg = p->les_zavg; d.thermal = p->thermal;
+    d.refine_sweeps = p->refine_sweeps < 1 ? 1 : p->refine_sweeps;
+    if (p->precision == FVM_MIXED)
+        d.nswpp = ((p->nswpp + d.refine_sweeps - 1) / d.refine_sweeps) * d.refine_sweeps;
     cudaError_t e = cudaSetDevice(p->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_pctl, sizeof(fvm::PCtl));
@@ -1866,9 +2007,15 @@ int fvm3_time_sweeps(fvm3_ctx *c, int sweeps, double *ms_per_sweep)
     // the sweeps of the loop body on a scratch copy of P (SU as left by the last step)
     F3CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int rc = FVM_OK;
+    const bool mixed = c->p.precision == FVM_MIXED;
     for (int s = 0; s < sweeps && rc == FVM_OK; s++) {
-        rc = f3::line(c, 6, d.SU, d.DIVDT, 0);
-        if (rc == FVM_OK) rc = f3::line(c, 6, d.SU, d.DIVDT, 1);
+        if (mixed) {
+            rc = f3::line32(c, 0, 0);
+            if (rc == FVM_OK) rc = f3::line32(c, 1, 0);
+        } else {
+            rc = f3::line(c, 6, d.SU, d.DIVDT, 0);
+            if (rc == FVM_OK) rc = f3::line(c, 6, d.SU, d.DIVDT, 1);
+        }
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc || e != cudaSuccess) {

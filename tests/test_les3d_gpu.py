@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle
-from fvm_gb300 import capi3d
+from fvm_gb300 import capi, capi3d
 from fvm_gb300.grid import o_grid_3d, perturbation_3d
 from tests.helpers import rel_l2
 
@@ -14,7 +14,8 @@ pytestmark = pytest.mark.gpu
 GEOM = ["DJAC", "XIX", "XIY", "XIZ", "ETX", "ETY", "ETZ", "ZTX", "ZTY", "ZTZ", "DE", "DN", "DT", "THETA"]
 
 
-def _case(skew=0.3, les=True, zavg=False, thermal=True, re=3900.0, resimax=1e-11, nswpp=20000):
+def _case(skew=0.3, les=True, zavg=False, thermal=True, re=3900.0, resimax=1e-11, nswpp=20000, precision=0,
+          refine_sweeps=8):
     g = o_grid_3d(16, 12, 8, lz=np.pi, dr1=0.01, skew=skew)
     du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, 0.05, 3)
     kw = dict(re=re, dt=0.002, resimax=resimax, nswpp=nswpp, use_les=les, les_zavg=zavg, thermal=thermal,
@@ -23,7 +24,8 @@ def _case(skew=0.3, les=True, zavg=False, thermal=True, re=3900.0, resimax=1e-11
     o.set_grid(g)
     o.init(du, dv, dw)
     p = capi3d.default_params(ni=g.ni, nj=g.nj, nk=g.nk, re=re, dt=0.002, resimax=resimax, nswpp=nswpp,
-                              use_les=int(les), les_zavg=int(zavg), thermal=int(thermal), res_every=2, ref_a=np.pi)
+                              use_les=int(les), les_zavg=int(zavg), thermal=int(thermal), res_every=2, ref_a=np.pi,
+                              precision=precision, refine_sweeps=refine_sweeps)
     ctx = capi3d.Context3(p)
     ctx.set_grid(g)
     ctx.init(du, dv, dw)
@@ -66,3 +68,24 @@ def test_steps_match_the_restatement(les):
         assert c["sweeps"] == co["sweeps"], s
     for nm in ("U", "V", "W", "P", "T"):
         assert rel_l2(ctx.get(nm), o.array(nm), interior_of=None) <= 1e-9, nm
+
+
+@pytest.mark.parametrize("refine", [4, 8])
+def test_mixed_poisson_matches_fp64(refine):
+    """FP32 correction sweeps inside FP64 residual refinement converge to the FP64
+    fixed point: fields and drag within 1e-6 of the FP64 restatement."""
+    g, o, ctx = _case(precision=capi.MIXED, refine_sweeps=refine)
+    for s in range(3):
+        o.step(1)
+        c = ctx.step(1)
+        co = o.coeffs()
+        assert c["cd"] == pytest.approx(co["cd"], rel=1e-6), s
+        assert c["resid"] <= 1e-11 and c["sweeps"] % refine == 0, s
+    for nm in ("U", "V", "W", "P", "T"):
+        assert rel_l2(ctx.get(nm), o.array(nm), interior_of=None) <= 1e-6, nm
+
+
+def test_mixed_sweep_cap_is_reported():
+    g, o, ctx = _case(precision=capi.MIXED, refine_sweeps=8, resimax=1e-30, nswpp=40)
+    c = ctx.step(1)
+    assert c["sweeps"] == 40 and c["resid"] > 1e-30
