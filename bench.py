@@ -388,7 +388,7 @@ def run_adjoint_bench(args):
 # 3-D LES (include/fvm3d.h) on the 256 theta x 192 r x 48 z O-grid, FP64 and mixed
 # ---------------------------------------------------------------------------------
 LES3D = dict(name="les3d-re3900-256x192x48", n_theta=256, n_r=192, n_z=48, re=3900.0, pr=0.71, dt=0.002,
-             dr1=0.001, amp=0.05, seed=0, resimax=1e-8, nswpp=3000, res_every=4, refine_sweeps=16, zavg=1,
+             dr1=0.001, amp=0.05, seed=0, resimax=1e-10, nswpp=200, res_every=4, refine_sweeps=20, zavg=1,
              thermal=1)
 FIELDS3D = ("U", "V", "W", "P", "T", "NLX", "NLY", "NLZ", "ADV")
 

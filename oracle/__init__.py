@@ -33,6 +33,15 @@ class Coeffs(ctypes.Structure):
                [("sweeps", ctypes.c_int), ("resid", ctypes.c_double)]
 
 
+class Post(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("time", "nu", "cd", "cl", "cl_amp", "cpb", "st", "rms_cd", "rms_cl", "st_last", "cl_amp_last")] + \
+               [("niter", ctypes.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 def build(force: bool = False) -> str:
     """Compile the restatement with its Makefile (portable flags, no FMA contraction)."""
     src = os.path.join(HERE, "fvm_oracle.c")
@@ -67,6 +76,11 @@ def lib():
         L.orc_sum_area.restype = ctypes.c_double
         L.orc_sum_area.argtypes = [ctypes.c_void_p]
         L.orc_iter_p.restype = ctypes.c_int
+        L.orc_post_begin.argtypes = [ctypes.c_void_p]
+        L.orc_calc_vor.argtypes = [ctypes.c_void_p]
+        L.orc_post_record.restype = ctypes.POINTER(Post)
+        L.orc_post_record.argtypes = [ctypes.c_void_p]
+        L.orc_post_final.argtypes = [ctypes.c_void_p, ctypes.POINTER(Post), P, P, P, P, P]
         for f in ("orc_begin_step", "orc_contra_vel", "orc_explicit", "orc_iter_u", "orc_iter_v",
                   "orc_remove_grad", "orc_iter_p", "orc_correct", "orc_iter_t", "orc_calccoef"):
             getattr(L, f).argtypes = [ctypes.c_void_p]
@@ -148,6 +162,22 @@ class Oracle:
     def coeffs(self) -> dict:
         c = lib().orc_last_coeffs(self._h).contents
         return {n: getattr(c, n) for n, _ in Coeffs._fields_}
+
+    def post_begin(self):
+        """POST_PROCESS with IPOST=0: time averaging from the next step on."""
+        lib().orc_post_begin(self._h)
+
+    def post_record(self) -> dict:
+        """The POST_NU_CD_CL.PLT record of the last step."""
+        return lib().orc_post_record(self._h).contents.as_dict()
+
+    def post_final(self):
+        """POST_PROCESS with IPOST=1: averaged coefficients and fields."""
+        out = Post()
+        shape = (self.nj + 1, self.ni + 1)
+        f = {nm: np.zeros(shape) for nm in ("U", "V", "P", "T", "VOR")}
+        lib().orc_post_final(self._h, ctypes.byref(out), *[_dptr(f[nm]) for nm in ("U", "V", "P", "T", "VOR")])
+        return out.as_dict(), f
 
     @property
     def time(self):

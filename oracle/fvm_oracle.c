@@ -32,6 +32,12 @@ struct orc {
     double *la, *lb, *lc, *ld, *lx, *lz, *lw, *lu, *lbb;
     /* wall controls (no reference counterpart): wall-normal blowing speed per J */
     double *BLOW;
+    /* post-processing (comdat_shared.f90:149-160) */
+    double *VOR, *U_TA, *V_TA, *P_TA, *T_TA, *VOR_TA;
+    int ipost, toggle, niter_pos;
+    double cl_nm1, cl1, st, cl_amp, time1, time2;
+    double nu_ta, cd_ta, cl_ta, st_ta, cpb_ta, cl_amp_ta, rms_cd, rms_cl;
+    orc_post post;
     orc_coeffs co;
 };
 
@@ -57,7 +63,8 @@ orc *orc_create(const orc_params *p)
                        &o->V_N, &o->T_N, &o->NLX, &o->NLY, &o->ADV, &o->NLX_NM1, &o->NLY_NM1,
                        &o->ADV_NM1, &o->DIFX, &o->DIFY, &o->DIFT, &o->S_U, &o->S_V, &o->U1,
                        &o->U2, &o->UE, &o->UW, &o->VN, &o->VS, &o->AP, &o->AE, &o->AW,
-                       &o->AN, &o->AS, &o->SU, &o->DD};
+                       &o->AN, &o->AS, &o->SU, &o->DD, &o->VOR, &o->U_TA, &o->V_TA, &o->P_TA,
+                       &o->T_TA, &o->VOR_TA};
     for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); k++) {
         *arrs[k] = zalloc(o->n);
         if (!*arrs[k]) { orc_destroy(o); return NULL; }
@@ -83,7 +90,8 @@ void orc_destroy(orc *o)
                       o->ADV, o->NLX_NM1, o->NLY_NM1, o->ADV_NM1, o->DIFX, o->DIFY, o->DIFT,
                       o->S_U, o->S_V, o->U1, o->U2, o->UE, o->UW, o->VN, o->VS, o->AP, o->AE,
                       o->AW, o->AN, o->AS, o->SU, o->DD, o->la, o->lb, o->lc, o->ld, o->lx, o->lz,
-                      o->lw, o->lu, o->lbb, o->BLOW};
+                      o->lw, o->lu, o->lbb, o->BLOW, o->VOR, o->U_TA, o->V_TA, o->P_TA, o->T_TA,
+                      o->VOR_TA};
     for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); k++) free(arrs[k]);
     free(o);
 }
@@ -763,6 +771,123 @@ void orc_iter_t(orc *o)
     bct(o);
 }
 
+/* CALC_VOR (calc_vor.f90:14-58): cell-centre vorticity, one-sided (extrapolated
+ * ghost) differences on the I=0 and I=NI rows, branch-cut rows copied. */
+void orc_calc_vor(orc *o)
+{
+    const int NI = o->NI, NJ = o->NJ;
+    const double *U = o->U, *V = o->V;
+    double *W = o->VOR;
+    for (int j = 1; j <= NJ - 1; j++)
+        for (int i = 1; i <= NI - 1; i++) {
+            const int c = ID(i, j);
+            W[c] = (((o->XIX[c] * 0.5) * (V[ID(i + 1, j)] - V[ID(i - 1, j)]) +
+                     (o->ETX[c] * 0.5) * (V[ID(i, j + 1)] - V[ID(i, j - 1)])) -
+                    (o->XIY[c] * 0.5) * (U[ID(i + 1, j)] - U[ID(i - 1, j)])) -
+                   (o->ETY[c] * 0.5) * (U[ID(i, j + 1)] - U[ID(i, j - 1)]);
+        }
+    for (int j = 1; j <= NJ - 1; j++) {
+        int i = 0, c = ID(i, j);
+        W[c] = (((o->XIX[c] * 0.5) * (V[ID(i + 1, j)] - ((3.0 * V[c] - 3.0 * V[ID(i + 1, j)]) + V[ID(i + 2, j)])) +
+                 (o->ETX[c] * 0.5) * (V[ID(i, j + 1)] - V[ID(i, j - 1)])) -
+                (o->XIY[c] * 0.5) * (U[ID(i + 1, j)] - ((3.0 * U[c] - 3.0 * U[ID(i + 1, j)]) + U[ID(i + 2, j)]))) -
+               (o->ETY[c] * 0.5) * (U[ID(i, j + 1)] - U[ID(i, j - 1)]);
+        i = NI;
+        c = ID(i, j);
+        W[c] = (((o->XIX[c] * 0.5) * (((3.0 * V[c] - 3.0 * V[ID(i - 1, j)]) + V[ID(i - 2, j)]) - V[ID(i - 1, j)]) +
+                 (o->ETX[c] * 0.5) * (V[ID(i, j + 1)] - V[ID(i, j - 1)])) -
+                (o->XIY[c] * 0.5) * (((3.0 * U[c] - 3.0 * U[ID(i - 1, j)]) + U[ID(i - 2, j)]) - U[ID(i - 1, j)])) -
+               (o->ETY[c] * 0.5) * (U[ID(i, j + 1)] - U[ID(i, j - 1)]);
+    }
+    for (int i = 0; i <= NI; i++) {
+        W[ID(i, 0)] = W[ID(i, NJ - 1)];
+        W[ID(i, NJ)] = W[ID(i, 1)];
+    }
+}
+
+/* POST_PROCESS, IPOST=0 branch (post_process.f90:8-16). */
+void orc_post_begin(orc *o)
+{
+    o->niter_pos = 0;
+    o->toggle = 1;
+    o->ipost = 1;
+}
+
+/* The post-processing block of CALCCOEF (calccoef.f90:156-190). */
+static void post_step(orc *o)
+{
+    orc_calc_vor(o);
+    o->niter_pos = o->niter_pos + 1;
+    const double cl = o->co.cl, rtime = o->rtime;
+    if ((double)o->toggle * (cl - o->cl_nm1) < 0.0) { /* lift extremum: half period */
+        o->toggle = -1 * o->toggle;
+        o->st = 1.0 / (rtime - o->time2);
+        o->time2 = o->time1;
+        o->time1 = rtime;
+        o->cl_amp = fabs(cl - o->cl1) / 2.0;
+        o->cl1 = cl;
+    }
+    for (int c = 0; c < o->n; c++) {
+        o->U_TA[c] = o->U_TA[c] + o->U[c];
+        o->V_TA[c] = o->V_TA[c] + o->V[c];
+        o->P_TA[c] = o->P_TA[c] + o->P[c];
+        o->T_TA[c] = o->T_TA[c] + o->T[c];
+        o->VOR_TA[c] = o->VOR_TA[c] + o->VOR[c];
+    }
+    o->nu_ta = o->nu_ta + o->co.nu;
+    o->cd_ta = o->cd_ta + o->co.cd;
+    o->cl_ta = o->cl_ta + cl;
+    o->st_ta = o->st_ta + o->st;
+    o->cpb_ta = o->cpb_ta + o->co.cpb;
+    o->cl_amp_ta = o->cl_amp_ta + o->cl_amp;
+    const double n = (double)o->niter_pos;
+    const double dum_a = o->cd_ta / n, dum_b = o->cl_ta / n;
+    o->rms_cd = o->rms_cd + (o->co.cd - dum_a) * (o->co.cd - dum_a);
+    o->rms_cl = o->rms_cl + (cl - dum_b) * (cl - dum_b);
+    orc_post *r = &o->post;
+    r->time = rtime;
+    r->nu = o->nu_ta / n;
+    r->cd = dum_a;
+    r->cl = dum_b;
+    r->cl_amp = o->cl_amp_ta / n;
+    r->cpb = o->cpb_ta / n;
+    r->st = o->st_ta / n;
+    r->rms_cd = sqrt(o->rms_cd / n);
+    r->rms_cl = sqrt(o->rms_cl / n);
+    r->st_last = o->st;
+    r->cl_amp_last = o->cl_amp;
+    r->niter = o->niter_pos;
+}
+
+const orc_post *orc_post_record(const orc *o) { return &o->post; }
+
+/* POST_PROCESS, IPOST=1 branch (post_process.f90:19-36). */
+void orc_post_final(orc *o, orc_post *out, double *u, double *v, double *p, double *t, double *vor)
+{
+    const double n = (double)o->niter_pos;
+    for (int c = 0; c < o->n; c++) {
+        if (u) u[c] = o->U_TA[c] / n;
+        if (v) v[c] = o->V_TA[c] / n;
+        if (p) p[c] = o->P_TA[c] / n;
+        if (t) t[c] = o->T_TA[c] / n;
+        if (vor) vor[c] = o->VOR_TA[c] / n;
+    }
+    if (out) {
+        out->time = o->rtime;
+        out->nu = o->nu_ta / n;
+        out->cd = o->cd_ta / n;
+        out->cl = o->cl_ta / n;
+        out->st = o->st_ta / n;
+        out->cpb = o->cpb_ta / n;
+        out->cl_amp = o->cl_amp_ta / n;
+        out->rms_cd = sqrt(o->rms_cd / n);
+        out->rms_cl = sqrt(o->rms_cl / n);
+        out->st_last = o->st;
+        out->cl_amp_last = o->cl_amp;
+        out->niter = o->niter_pos;
+    }
+}
+
 /* CALCCOEF (calccoef.f90:9-120): CFL, base pressure, wall forces, Nusselt. */
 void orc_calccoef(orc *o)
 {
@@ -814,6 +939,7 @@ void orc_calccoef(orc *o)
         t_lift = t_lift - (((2.0 / o->p.re) * dudn) * ar) * cos(th);
         sum_nu = sum_nu + dtdn * ar;
     }
+    o->cl_nm1 = o->co.cl; /* calccoef.f90:109 */
     o->co.time = o->rtime;
     o->co.cfl = cfl;
     o->co.cpb = cpb;
@@ -824,6 +950,7 @@ void orc_calccoef(orc *o)
     o->co.cd = p_drag + t_drag;
     o->co.cl = p_lift + t_lift;
     o->co.nu = -sum_nu / o->sum_area;
+    if (o->ipost) post_step(o);
 }
 
 int orc_step(orc *o, int nsteps)
@@ -863,7 +990,8 @@ double *orc_array(orc *o, const char *name)
         {"Q11", o->Q11}, {"Q12", o->Q12}, {"Q22", o->Q22}, {"DE", o->DE}, {"DW", o->DW},
         {"DN", o->DN}, {"DS", o->DS}, {"THETA", o->THETA}, {"AREA", o->AREA}, {"AP", o->AP},
         {"AE", o->AE}, {"AW", o->AW}, {"AN", o->AN}, {"AS", o->AS}, {"SU", o->SU}, {"DD", o->DD},
-        {"U1", o->U1}, {"U2", o->U2}};
+        {"U1", o->U1}, {"U2", o->U2}, {"VOR", o->VOR}, {"U_TA", o->U_TA}, {"V_TA", o->V_TA},
+        {"P_TA", o->P_TA}, {"T_TA", o->T_TA}, {"VOR_TA", o->VOR_TA}};
     for (size_t k = 0; k < sizeof(t) / sizeof(t[0]); k++)
         if (strcmp(t[k].n, name) == 0) return t[k].a;
     return NULL;

@@ -60,6 +60,16 @@ typedef struct {
     double resid;        /* final scaled residual of the last step */
 } orc_coeffs;
 
+/* Record of the post-processing phase: what CALCCOEF appends to
+ * POST_NU_CD_CL.PLT after each step (calccoef.f90:186-188) -- time averages of
+ * Nu, Cd, Cl, the lift half-amplitude, Cpb and St, and the rms of Cd and Cl about
+ * the running means -- plus ST and CL_AMP of the last detected extremum pair. */
+typedef struct {
+    double time, nu, cd, cl, cl_amp, cpb, st, rms_cd, rms_cl;
+    double st_last, cl_amp_last;
+    int niter;           /* NITER_POS: steps averaged */
+} orc_post;
+
 typedef struct orc orc;
 
 orc *orc_create(const orc_params *p);
@@ -91,11 +101,28 @@ void orc_calccoef(orc *o);        /* calccoef.f90 */
  * entering the wall velocity of BCU/BCV and the wall face flux UW(1,J). */
 void orc_set_controls(orc *o, double omega, const double *blow);
 
+/* Post-processing (no effect on the flow).
+ * orc_post_begin: POST_PROCESS with IPOST=0 (post_process.f90:8-16): NITER_POS=0,
+ *   TOGGLE=1, averaging on from the next step.  The other post variables (ST,
+ *   CL_AMP, CL1, TIME1, TIME2 and the sums) keep their values, zero at creation.
+ * Every CALCCOEF while averaging runs calccoef.f90:156-190: CALC_VOR, the lift
+ *   extremum test that sets ST and CL_AMP, the sums of U,V,P,T,VOR and of the
+ *   coefficients, and the rms sums.
+ * orc_post_final: POST_PROCESS with IPOST=1 (post_process.f90:19-36): averages
+ *   into *out and the averaged fields into u,v,p,t,vor (any may be NULL); the
+ *   reference overwrites its state with them at the end of the run, the oracle
+ *   leaves the state alone.
+ * orc_calc_vor: CALC_VOR (calc_vor.f90:14-58) into "VOR". */
+void orc_post_begin(orc *o);
+const orc_post *orc_post_record(const orc *o);
+void orc_post_final(orc *o, orc_post *out, double *u, double *v, double *p, double *t, double *vor);
+void orc_calc_vor(orc *o);
+
 /* Raw access to any named array (NULL if unknown).  Names: "U","V","P","T",
  * "U_N","V_N","T_N","NLX","NLY","ADV","NLX_NM1","NLY_NM1","ADV_NM1","DIFX",
  * "DIFY","DIFT","S_U","S_V","UE","UW","VN","VS","X","Y","XG","YG","XIX","XIY",
  * "ETX","ETY","DJAC","Q11","Q12","Q22","DE","DW","DN","DS","THETA","AREA",
- * "AP","AE","AW","AN","AS","SU","DD". */
+ * "AP","AE","AW","AN","AS","SU","DD","VOR","U_TA","V_TA","P_TA","T_TA","VOR_TA". */
 double *orc_array(orc *o, const char *name);
 int orc_size(const orc *o);         /* (NI+1)*(NJ+1) */
 double orc_time(const orc *o);

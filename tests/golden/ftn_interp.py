@@ -806,7 +806,10 @@ def exec_stmt(M, s, env):
         unit = int(m.group(2))
         fm = re.search(r"FILE\s*=\s*'([^']*)'", s[2], re.I)
         M.units_open[unit] = fm.group(1) if fm else None
-        M.unit_out.setdefault(unit, [])
+        if re.search(r"ACCESS\s*=\s*'APPEND'", s[2], re.I):
+            M.unit_out.setdefault(unit, [])
+        else:   # a sequential file opened without APPEND is written from its start
+            M.unit_out[unit] = []
     elif t == "write":
         unit = s[2]
         if unit == "*" or not unit.isdigit():

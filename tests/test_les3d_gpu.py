@@ -14,7 +14,9 @@ pytestmark = pytest.mark.gpu
 GEOM = ["DJAC", "XIX", "XIY", "XIZ", "ETX", "ETY", "ETZ", "ZTX", "ZTY", "ZTZ", "DE", "DN", "DT", "THETA"]
 
 
-def _case(skew=0.3, les=True, zavg=False, thermal=True, re=3900.0, resimax=1e-11, nswpp=20000, precision=0,
+# the I-line Poisson iteration needs 7e4-8e4 sweeps per step to reach 1e-11 on this
+# grid (the J and K couplings are explicit); the cap is above that
+def _case(skew=0.3, les=True, zavg=False, thermal=True, re=3900.0, resimax=1e-11, nswpp=120000, precision=0,
           refine_sweeps=8):
     g = o_grid_3d(16, 12, 8, lz=np.pi, dr1=0.01, skew=skew)
     du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, 0.05, 3)
@@ -65,7 +67,7 @@ def test_steps_match_the_restatement(les):
         c = ctx.step(1)
         co = o.coeffs()
         assert c["cd"] == pytest.approx(co["cd"], rel=1e-9), s
-        assert c["sweeps"] == co["sweeps"], s
+        assert c["sweeps"] == co["sweeps"] and c["resid"] <= 1e-11, s
     for nm in ("U", "V", "W", "P", "T"):
         assert rel_l2(ctx.get(nm), o.array(nm), interior_of=None) <= 1e-9, nm
 
