@@ -475,7 +475,9 @@ def run_les3d_bench(args):
     if os.path.exists(pk):
         peaks = json.load(open(pk))
     res = {}
-    for name, prec in (("mixed", capi.MIXED), ("fp64", capi.FP64)):
+    parts = {"all": (("mixed", capi.MIXED), ("fp64", capi.FP64)), "mixed": (("mixed", capi.MIXED),),
+             "fp64": (("fp64", capi.FP64),)}[args.parts]
+    for name, prec in parts:
         ctx = make_ctx3(w, prec, local, g, du, dv, dw)
         ext = torch.cuda.ExternalStream(ctx.stream_handle())
         t0 = time.perf_counter()
@@ -508,6 +510,14 @@ def run_les3d_bench(args):
         print(f"les3d {name}: {ms / args.steps:.1f} ms/step, sweeps {sweeps}, sweep pair {sweep_ms * 1e3:.1f} us",
               file=sys.stderr, flush=True)
         ctx.close()
+    if args.parts != "all":   # profiling runs: one precision only
+        if rank == 0:
+            nm = parts[0][0]
+            print(json.dumps({"metric": METRIC, "workload": w["name"], "parts": nm,
+                              "ms_per_step": res[nm]["ms"] / args.steps,
+                              "sweep_pair_us": res[nm]["sweep_ms"] * 1e3}), flush=True)
+        dist.finalize()
+        return
     # e2e through the C-ABI with pinned host buffers (mixed path)
     ctx = make_ctx3(w, capi.MIXED, local, g, du, dv, dw)
     ext = torch.cuda.ExternalStream(ctx.stream_handle())
@@ -732,8 +742,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--parts", choices=["all", "mixed"], default="all",
-                    help="'mixed' times only the headline path (for profiler runs)")
+    ap.add_argument("--parts", choices=["all", "mixed", "fp64"], default="all",
+                    help="'mixed' / 'fp64' time one precision only (profiler runs; fp64: les3d only)")
     ap.add_argument("--workload", choices=["cylinder2d", "sweep64", "adjoint", "les3d"], default="cylinder2d",
                     help="sweep64: 64 ragged cases advanced as batches, sharded over the ranks; "
                          "adjoint: window-drag gradient on the 128x96 grid; "

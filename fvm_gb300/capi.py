@@ -29,7 +29,8 @@ EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", 
            "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps", "fvm_poisson_residual_static",
            "fvm_batch_create", "fvm_batch_destroy", "fvm_batch_last_error", "fvm_batch_case",
            "fvm_batch_tiles", "fvm_batch_set_tiles", "fvm_batch_autotune", "fvm_batch_time_sweeps",
-           "fvm_batch_step", "fvm_batch_get_timing"]
+           "fvm_batch_step", "fvm_batch_get_timing", "fvm_post_begin", "fvm_post_get", "fvm_post_final",
+           "fvm_post_end", "fvm_calc_vor"]
 
 
 class Params(ctypes.Structure):
@@ -50,6 +51,15 @@ class Coeffs(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in
                 ("time", "cfl", "cpb", "cd", "cl", "cd_p", "cd_v", "cl_p", "cl_v", "nu")] + \
                [("sweeps", ctypes.c_int), ("resid", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Post(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("time", "nu", "cd", "cl", "cl_amp", "cpb", "st", "rms_cd", "rms_cl", "st_last", "cl_amp_last")] + \
+               [("niter", ctypes.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -104,6 +114,10 @@ def load(build_if_missing: bool = True):
     L.fvm_set_time.argtypes = [V, ctypes.c_double, ctypes.c_int]
     L.fvm_set_controls.argtypes = [V, ctypes.c_double, D]
     L.fvm_adjoint_drag_grad.argtypes = [V, ctypes.c_int, ctypes.c_int, D, D, D]
+    for f in ("fvm_post_begin", "fvm_post_end", "fvm_calc_vor"):
+        getattr(L, f).argtypes = [V]
+    L.fvm_post_get.argtypes = [V, ctypes.POINTER(Post)]
+    L.fvm_post_final.argtypes = [V, ctypes.POINTER(Post), D, D, D, D, D]
     L.fvm_adjoint_vjp.argtypes = [V, D, D, D, D, D, D]
     for f in ("fvm_begin_step", "fvm_contra_vel", "fvm_p_source", "fvm_iter_u", "fvm_iter_v",
               "fvm_remove_grad", "fvm_correct", "fvm_iter_t", "fvm_synchronize"):
@@ -229,6 +243,32 @@ class Context:
         """Wall rotation rate and wall-normal blowing speeds (NJ-1 values)."""
         b = None if blow is None else _arr(blow, self.nj - 1)
         self._ok(self.L.fvm_set_controls(self.h, omega, _dp(b)))
+
+    def post_begin(self):
+        """POST_PROCESS with IPOST=0: time averaging from the next step on."""
+        self._ok(self.L.fvm_post_begin(self.h))
+
+    def post_get(self) -> dict:
+        """The POST_NU_CD_CL.PLT record of the last step."""
+        r = Post()
+        self._ok(self.L.fvm_post_get(self.h, ctypes.byref(r)))
+        return r.as_dict()
+
+    def post_final(self):
+        """POST_PROCESS with IPOST=1: averaged coefficients and fields (the state
+        is left unchanged)."""
+        r = Post()
+        f = {nm: np.zeros((self.nj + 1, self.ni + 1)) for nm in ("U", "V", "P", "T", "VOR")}
+        self._ok(self.L.fvm_post_final(self.h, ctypes.byref(r), *[_dp(f[nm]) for nm in ("U", "V", "P", "T", "VOR")]))
+        return r.as_dict(), f
+
+    def post_end(self):
+        self._ok(self.L.fvm_post_end(self.h))
+
+    def calc_vor(self) -> np.ndarray:
+        """CALC_VOR of the current state."""
+        self._ok(self.L.fvm_calc_vor(self.h))
+        return self.get("VOR")
 
     def adjoint_drag_grad(self, window, ckpt=50):
         """Runs `window` steps from the current state; returns (J, dJ/domega,

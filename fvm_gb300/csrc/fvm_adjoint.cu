@@ -1147,6 +1147,13 @@ int run_adjoint(fvm_ctx *c, int window, int ckpt, double *J, double *dJ_domega, 
     ARC(state_copy(c, A->fin, true));
     const double t_end = c->rtime;
     const int it_end = c->niter_time;
+    const fvm_coeffs last_end = c->last;
+    // the recomputation passes repeat steps already taken: no post-processing
+    struct Suspend {
+        fvm_ctx *c;
+        explicit Suspend(fvm_ctx *cc) : c(cc) { c->post_suspend++; }
+        ~Suspend() { c->post_suspend--; }
+    } suspend(c);
     // reverse pass, one segment at a time
     ARC(adj_zero(c));
     for (int seg = nck - 1; seg >= 0; seg--) {
@@ -1171,6 +1178,7 @@ int run_adjoint(fvm_ctx *c, int window, int ckpt, double *J, double *dJ_domega, 
     ARC(state_copy(c, A->fin, false));
     c->rtime = t_end;
     c->niter_time = it_end;
+    c->last = last_end;
     FVM_CUDA(c, cudaStreamSynchronize(c->stream));
     return status;
 }

@@ -117,6 +117,7 @@ int fvm_destroy(fvm_ctx *c)
     if (!c) return FVM_ERR_ARG;
     if (c->stream) cudaStreamSynchronize(c->stream);
     fvm::adj_destroy(c);
+    fvm::post_free(c);
     if (c->pgraph) cudaGraphExecDestroy(c->pgraph);
     if (c->slab) cudaFree(c->slab);
     if (c->h_pctl) cudaFreeHost(c->h_pctl);
@@ -336,7 +337,7 @@ double *array_by_name(fvm_ctx *c, const char *name)
         {"SU", d.SU}, {"SUV", d.SUV}, {"SUT", d.SUT}, {"DD", d.DD}};
     for (auto &e : t)
         if (std::strcmp(e.n, name) == 0) return e.a;
-    return nullptr;
+    return post_array(c, name);
 }
 
 }  // namespace fvm

@@ -126,6 +126,19 @@ __device__ __forceinline__ const Dev &dev_of(const DevTable &t) { return t.devs[
 
 struct fvm_adj;   // adjoint storage (fvm_adjoint.cu), created on first use
 
+namespace fvm {
+// Post-processing state of CALCCOEF / POST_PROCESS (comdat_shared.f90:149-160):
+// the scalars on the host, the field sums on the device.
+struct PostState {
+    int ipost = 0, toggle = 0, niter_pos = 0;
+    double cl1 = 0.0, st = 0.0, cl_amp = 0.0, time1 = 0.0, time2 = 0.0;
+    double nu_ta = 0.0, cd_ta = 0.0, cl_ta = 0.0, st_ta = 0.0, cpb_ta = 0.0, cl_amp_ta = 0.0;
+    double rms_cd = 0.0, rms_cl = 0.0;
+    fvm_post rec{};
+    double *arr = nullptr;   // device: VOR, U_TA, V_TA, P_TA, T_TA, VOR_TA (n each)
+};
+}  // namespace fvm
+
 struct fvm_ctx {
     fvm_params p{};
     int NI = 0, NJ = 0, NI1 = 0, n = 0;
@@ -151,6 +164,8 @@ struct fvm_ctx {
     bool capturing = false;
     fvm_timing tm{};
     fvm_adj *adj = nullptr;
+    fvm::PostState post;
+    int post_suspend = 0;   // recomputation passes of the adjoint: no post-processing
 };
 
 // Count one kernel launch of the context (into the graph being captured, if any).
@@ -221,6 +236,11 @@ int run_iter_p(fvm_ctx *c, double *resid, int *sweeps);
 int run_correct(fvm_ctx *c);
 int run_iter_t(fvm_ctx *c);
 int run_calccoef(fvm_ctx *c, fvm_coeffs *out);
+// post-processing block of CALCCOEF for a step whose record is co; cl_prev is
+// the previous step's lift (CL_NM1, calccoef.f90:109)
+int post_after_calccoef(fvm_ctx *c, double cl_prev, const fvm_coeffs &co);
+void post_free(fvm_ctx *c);
+double *post_array(fvm_ctx *c, const char *name);
 int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out);
 double *array_by_name(fvm_ctx *c, const char *name);
 int run_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches);

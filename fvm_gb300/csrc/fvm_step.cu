@@ -1034,7 +1034,11 @@ int run_calccoef(fvm_ctx *c, fvm_coeffs *out)
     LAUNCH_S(t, k_calc_rows, dim3((t.NJ + 127) / 128, 1, 1), 128);
     LAUNCH_S(t, k_cfl, interior_grid(t), 128);
     LAUNCH_S(t, k_calc_final, dim3(1, 1, 1), 1, c->rtime, dout);
-    return calccoef_copy(c, dout, out);
+    const double cl_prev = c->last.cl;   // CL_NM1 (calccoef.f90:109)
+    fvm_coeffs co;
+    RC(calccoef_copy(c, dout, &co));
+    if (out) *out = co;
+    return post_after_calccoef(c, cl_prev, co);
 }
 
 int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out)
@@ -1049,8 +1053,10 @@ int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out)
         RC(poisson_loop(c));
         fvm_coeffs *dout = coef_slot(c);
         RC(step_after_poisson(t, c->rtime, dout));
+        const double cl_prev = c->last.cl;   // CL_NM1 (calccoef.f90:109)
         fvm_coeffs co;
         RC(calccoef_copy(c, dout, &co));
+        RC(post_after_calccoef(c, cl_prev, co));
         c->tm.kernel_launches += poisson_loop_kernels(c, co.sweeps);
         c->tm.sweeps += co.sweeps;
         if (!std::isfinite(co.resid)) {

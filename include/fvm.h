@@ -113,6 +113,37 @@ int fvm_set_time(struct fvm_ctx *ctx, double rtime, int niter_time);
  * reference's. */
 int fvm_set_controls(struct fvm_ctx *ctx, double omega, const double *blow);
 
+/* Post-processing phase (calccoef.f90:156-190, post_process.f90:8-62,
+ * calc_vor.f90:14-58).
+ * fvm_post_begin: POST_PROCESS with IPOST=0 -- NITER_POS=0, TOGGLE=1, the sums
+ *   cleared; from the next step on, every CALCCOEF (fvm_step, fvm_calccoef)
+ *   runs CALC_VOR, the lift-extremum test (ST = 1/(t - t two extrema ago),
+ *   CL_AMP = |CL - CL at the last extremum|/2), adds U,V,P,T,VOR to their time
+ *   sums on the device and Nu,Cd,Cl,St,Cpb,CL_AMP and the squared deviations of
+ *   Cd, Cl from their running means to host sums.
+ * fvm_post_get: the record CALCCOEF appends to POST_NU_CD_CL.PLT for the last
+ *   step (calccoef.f90:186-188).
+ * fvm_post_final: POST_PROCESS with IPOST=1 -- the averages (the
+ *   TIME_AVERAGED_RESULTS.DAT record) and the time-averaged fields of
+ *   TIME-AVERAGED FIELD.PLT into host arrays (any may be NULL).  Unlike the
+ *   reference, which overwrites its state with the averages at the end of its
+ *   run, the state is left unchanged.
+ * fvm_post_end: averaging off.
+ * fvm_calc_vor: CALC_VOR into the array "VOR" (fvm_get_array).  The sums are
+ *   readable as "U_TA", "V_TA", "P_TA", "T_TA", "VOR_TA" once averaging began. */
+typedef struct fvm_post {
+    double time, nu, cd, cl, cl_amp, cpb, st, rms_cd, rms_cl;
+    double st_last, cl_amp_last;   /* ST and CL_AMP of the last extremum pair */
+    int niter;                     /* NITER_POS: steps averaged */
+} fvm_post;
+
+int fvm_post_begin(struct fvm_ctx *ctx);
+int fvm_post_get(struct fvm_ctx *ctx, fvm_post *out);
+int fvm_post_final(struct fvm_ctx *ctx, fvm_post *out, double *u, double *v, double *p, double *t,
+                   double *vor);
+int fvm_post_end(struct fvm_ctx *ctx);
+int fvm_calc_vor(struct fvm_ctx *ctx);
+
 /* Discrete adjoint (no reference counterpart).  From the current state, runs
  * `window` steps (the state advances, as fvm_step would) and returns
  * J = mean over those steps of the drag coefficient CALCCOEF reports, with its

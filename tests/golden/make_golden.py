@@ -1,7 +1,7 @@
 """Generate the golden fixtures by running the reference's own Fortran sources.
 
 Usage (only where the reference tree exists):
-    python tests/golden/make_golden.py /root/reference [--3d-only]
+    python tests/golden/make_golden.py /root/reference [--3d-only | --program-only]
 
 For each case the R2D snapshot (cylinder/cylinder_v3.0.3_AF_original 4step_face_nl)
 is executed by ftn_interp with NI, NJ (and where stated NSWPP, RESIMAX) replaced in
@@ -56,6 +56,46 @@ CASES = [
     dict(name="polar_16x12_re80_tight", n_theta=16, n_r=12, skew=0.0, re=80.0, pr=0.71, vel_rot=0.0, dt=0.005,
          steps=3, over={"NSWPP": 100000, "RESIMAX": 1e-12}),
 ]
+
+
+# The whole 2-D program, time loop included: the loop runs to RTIME_MAX, POST_PROCESS
+# (IPOST=0) switches the averaging on and the loop continues to RTIME_END, with the
+# CALCCOEF post-processing block active; POST_PROCESS (IPOST=1) writes the averages.
+# RESTART.DAT is written every NITER_R steps.
+PROGRAM_CASES = [
+    dict(name="program_32x16_re100_rot_post", n_theta=32, n_r=16, skew=0.0, re=100.0, pr=0.71, vel_rot=0.3,
+         dt=0.005, steps_before=5, steps_post=8, niter_r=5),
+]
+
+
+def run_program_case(ref_root, c):
+    g = o_grid(c["n_theta"], c["n_r"], skew=c["skew"])
+    dt = c["dt"]
+    # half-step margins keep the RTIME comparisons of Main.f90:118 away from ties
+    over = {"NI": g.ni, "NJ": g.nj, "RTIME_MAX": (c["steps_before"] - 0.5) * dt,
+            "RTIME_END": (c["steps_before"] + c["steps_post"] - 0.5) * dt, "NITER_R": c["niter_r"]}
+    M = F.load_program(os.path.join(ref_root, SNAPSHOT), FILES, over)
+    M.stdin = [0, c["re"], c["pr"], c["vel_rot"], dt]
+    vals = []
+    for j in range(1, g.nj + 1):
+        for i in range(1, g.ni + 1):
+            vals += [float(g.xg[j, i]), float(g.yg[j, i])]
+    M.unit_in[10] = vals
+    F.run_stmts(M, M.subs["__MAIN__"].body, None)
+    out = {nm: M.g[nm].a[:, :, 0].T.copy() for nm in ("U", "V", "P", "T", "NLX", "NLY", "ADV")}
+
+    def numeric(unit, skip):
+        return np.array([r for r in M.unit_out.get(unit, [])[skip:]], dtype=np.float64)
+
+    out["COEFFS"] = numeric(11, 1)        # NU_CD_CL.PLT
+    out["POST"] = numeric(12, 1)          # POST_NU_CD_CL.PLT
+    out["FINAL"] = numeric(13, 1)         # TIME_AVERAGED_RESULTS.DAT
+    out["AVG_FIELD"] = numeric(41, 3)     # TIME-AVERAGED FIELD.PLT: x, y, u, v, P, vorticity, T
+    r16 = M.unit_out.get(16, [])          # RESTART.DAT of the last multiple of NITER_R
+    out["RESTART_HEAD"] = np.array(r16[0] + r16[1], dtype=np.float64)
+    out["RESTART_NL"] = np.array(r16[2::2], dtype=np.float64)
+    out["RESTART_STATE"] = np.array(r16[3::2], dtype=np.float64)
+    return g, out
 
 
 SNAPSHOT3D = os.path.join("LES", "v2.3_LES-Reynolds stresses")
@@ -144,11 +184,12 @@ def main():
     pos = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref_root = pos[0] if pos else "/root/reference"
     only3d = "--3d-only" in sys.argv
+    only_prog = "--program-only" in sys.argv
     manifest = []
-    if only3d:
+    if only3d or only_prog:
         with open(os.path.join(HERE, "manifest.json")) as f:
             manifest = json.load(f)["cases"]
-    for c in ([] if only3d else CASES):
+    for c in ([] if (only3d or only_prog) else CASES):
         t0 = time.time()
         g, out = run_case(ref_root, c)
         fn = f"{c['name']}.npz"
@@ -159,8 +200,22 @@ def main():
                              resimax=float(c["over"].get("RESIMAX", 1e-4)), amp=0.0, seed=0,
                              fields=["U", "V", "P", "T", "NLX", "NLY", "ADV"], order=0, tol=1e-12))
         print(f"{c['name']}: {time.time() - t0:.1f} s, {len(out['COEFFS'])} coefficient records", flush=True)
+    manifest_prog = []
+    for c in ([] if only3d else PROGRAM_CASES):
+        t0 = time.time()
+        g, out = run_program_case(ref_root, c)
+        fn = f"{c['name']}.npz"
+        np.savez_compressed(os.path.join(HERE, fn), **out)
+        manifest_prog.append(dict(c, file=fn, dr1=0.005, r_out=50.0, nswpp=20, resimax=1e-4))
+        print(f"{c['name']}: {time.time() - t0:.1f} s, {len(out['POST'])} post records", flush=True)
+    if only3d:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest_prog = json.load(f).get("program_cases", [])
     manifest3d = []
-    for c in CASES3D:
+    if only_prog:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest3d = json.load(f).get("cases3d", [])
+    for c in ([] if only_prog else CASES3D):
         t0 = time.time()
         g, out = run_case_3d(ref_root, c)
         fn = f"{c['name']}.npz"
@@ -173,7 +228,7 @@ def main():
         print(f"{c['name']}: {time.time() - t0:.1f} s, {len(out['COEFFS'])} coefficient records", flush=True)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py (reference sources executed by ftn_interp)",
-                   "cases": manifest, "cases3d": manifest3d}, f, indent=1)
+                   "cases": manifest, "program_cases": manifest_prog, "cases3d": manifest3d}, f, indent=1)
 
 
 if __name__ == "__main__":
