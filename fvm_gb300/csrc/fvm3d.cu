@@ -44,6 +44,7 @@ struct D3 {
     double *XG, *YG, *ZG, *X, *Y, *Z;
     double *XIX, *XIY, *XIZ, *ETX, *ETY, *ETZ, *ZTX, *ZTY, *ZTZ, *DJAC;
     double *Q11, *Q12, *Q13, *Q22, *Q23, *Q33;
+    double *JQ12, *JQ13, *JQ23;   // Q12*DJAC, Q13*DJAC, Q23*DJAC (the cross-term weights)
     double *DE, *DW, *DN, *DS, *DT, *DB, *THETA, *AREA1, *AREA2, *FW;
     double *MD[9];          // metric derivatives (scratch of the setup)
     // state
@@ -272,6 +273,9 @@ __global__ void k3_q(D3 d)
     d.Q23[c] = dot3(ex, zx, ey, zy, ez, zz);
     d.Q33[c] = dot3(zx, zx, zy, zy, zz, zz);
     d.FW[c] = pow(d.DJAC[c], 1.0 / 3.0);
+    d.JQ12[c] = d.Q12[c] * d.DJAC[c];
+    d.JQ13[c] = d.Q13[c] * d.DJAC[c];
+    d.JQ23[c] = d.Q23[c] * d.DJAC[c];
 }
 
 __global__ void k3_dcoef(D3 d)
@@ -495,23 +499,54 @@ __device__ __forceinline__ bool colour_line(const D3 &d, int fam, int colour, in
     return true;
 }
 
-__device__ __forceinline__ double couple(const D3 &d, const Coef3 &cf, const double *phi, int fam, int c)
+// Cell index of element 0 of line L, the element stride, and the offsets of the
+// four transverse neighbours (periodic wrap applied once per line).
+struct LineGeo {
+    int base, stride, o1, o2, o3, o4;
+};
+
+template <int FAM>
+__device__ __forceinline__ LineGeo line_geo(const D3 &d, int L)
 {
-    const int i = c % d.NI1, j = (c / d.NI1) % d.NJ1, k = c / (d.NI1 * d.NJ1);
-    if (fam == 0)
-        return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(cf.AN[c], phi[ID3(i, jw(d, j + 1), k)]),
-                                             __dmul_rn(cf.AS[c], phi[ID3(i, jw(d, j - 1), k)])),
-                                   __dmul_rn(cf.AT[c], phi[ID3(i, j, kw(d, k + 1))])),
-                         __dmul_rn(cf.AB[c], phi[ID3(i, j, kw(d, k - 1))]));
-    if (fam == 1)
-        return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(cf.AE[c], phi[ID3(i + 1, j, k)]),
-                                             __dmul_rn(cf.AW[c], phi[ID3(i - 1, j, k)])),
-                                   __dmul_rn(cf.AT[c], phi[ID3(i, j, kw(d, k + 1))])),
-                         __dmul_rn(cf.AB[c], phi[ID3(i, j, kw(d, k - 1))]));
-    return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(cf.AE[c], phi[ID3(i + 1, j, k)]),
-                                         __dmul_rn(cf.AW[c], phi[ID3(i - 1, j, k)])),
-                               __dmul_rn(cf.AN[c], phi[ID3(i, jw(d, j + 1), k)])),
-                     __dmul_rn(cf.AS[c], phi[ID3(i, jw(d, j - 1), k)]));
+    const int sj = d.NI1, sk = d.NI1 * d.NJ1;
+    LineGeo g;
+    if (FAM == 0) {   // I line (j, k): couplings N, S, T, B
+        const int j = L % (d.NJ - 1) + 1, k = L / (d.NJ - 1) + 1;
+        g.base = ID3(1, j, k);
+        g.stride = 1;
+        g.o1 = (jw(d, j + 1) - j) * sj;
+        g.o2 = (jw(d, j - 1) - j) * sj;
+        g.o3 = (kw(d, k + 1) - k) * sk;
+        g.o4 = (kw(d, k - 1) - k) * sk;
+    } else if (FAM == 1) {   // J line (i, k): couplings E, W, T, B
+        const int i = L % (d.NI - 1) + 1, k = L / (d.NI - 1) + 1;
+        g.base = ID3(i, 1, k);
+        g.stride = sj;
+        g.o1 = 1;
+        g.o2 = -1;
+        g.o3 = (kw(d, k + 1) - k) * sk;
+        g.o4 = (kw(d, k - 1) - k) * sk;
+    } else {   // K line (i, j): couplings E, W, N, S
+        const int i = L % (d.NI - 1) + 1, j = L / (d.NI - 1) + 1;
+        g.base = ID3(i, j, 1);
+        g.stride = sk;
+        g.o1 = 1;
+        g.o2 = -1;
+        g.o3 = (jw(d, j + 1) - j) * sj;
+        g.o4 = (jw(d, j - 1) - j) * sj;
+    }
+    return g;
+}
+
+// The four coupling coefficients of a family in the order of its neighbour offsets.
+template <int FAM>
+__device__ __forceinline__ void couple_coefs(const Coef3 &cf, const double *&c1, const double *&c2,
+                                             const double *&c3, const double *&c4)
+{
+    c1 = FAM == 0 ? cf.AN : cf.AE;
+    c2 = FAM == 0 ? cf.AS : cf.AW;
+    c3 = FAM == 2 ? cf.AN : cf.AT;
+    c4 = FAM == 2 ? cf.AS : cf.AB;
 }
 
 template <int M, int NW, int FAM>
@@ -528,14 +563,20 @@ __global__ void __launch_bounds__(128) k3_line(D3 d, LineSys s, Coef3 cf, const 
     const bool active = colour_line(d, FAM, colour, gl, L);
     if (!active) L = 0;
     const int n = s.n;
+    const LineGeo g = line_geo<FAM>(d, L);
+    const double *c1, *c2, *c3, *c4;
+    couple_coefs<FAM>(cf, c1, c2, c3, c4);
     double v[M];
 #pragma unroll
     for (int q = 0; q < M; q++) {
         const int e = q * TG + t;
         v[q] = 0.0;
         if (active && e < n) {
-            const int c = line_cell(d, FAM, L, e);
-            v[q] = __dadd_rn(couple(d, cf, phi, FAM, c), SU[c]);
+            const int c = g.base + e * g.stride;
+            const double cp = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(c1[c], phi[c + g.o1]), __dmul_rn(c2[c], phi[c + g.o2])),
+                                                  __dmul_rn(c3[c], phi[c + g.o3])),
+                                        __dmul_rn(c4[c], phi[c + g.o4]));
+            v[q] = __dadd_rn(cp, SU[c]);
         }
     }
     fvm::to_chunks<double, M, NW>(v, sm[gib], t);
@@ -546,7 +587,7 @@ __global__ void __launch_bounds__(128) k3_line(D3 d, LineSys s, Coef3 cf, const 
 #pragma unroll
     for (int q = 0; q < M; q++) {
         const int e = q * TG + t;
-        if (active && e < n) phi[line_cell(d, FAM, L, e)] = v[q];
+        if (active && e < n) phi[g.base + e * g.stride] = v[q];
     }
 }
 
@@ -604,9 +645,8 @@ __device__ __forceinline__ double nl3(const D3 &d, const double *in, int c, int 
 // DIF_DIAGONAL (dif_diagonal.f90:13-32): twelve cross terms with Q*J
 __device__ __forceinline__ double cross12(const D3 &d, const double *f, int i, int j, int k)
 {
-    const double *J = d.DJAC;
 #define F3(a, b, c) f[ID3(i + (a), j + (b), k + (c))]
-#define G3(Q, a, b, c) (d.Q[ID3(i + (a), j + (b), k + (c))] * J[ID3(i + (a), j + (b), k + (c))])
+#define G3(Q, a, b, c) (d.J##Q[ID3(i + (a), j + (b), k + (c))])
     double s = G3(Q12, 1, 0, 0) * (F3(1, 1, 0) - F3(1, -1, 0));
     s = s - G3(Q12, -1, 0, 0) * (F3(-1, 1, 0) - F3(-1, -1, 0));
     s = s + G3(Q13, 1, 0, 0) * (F3(1, 0, 1) - F3(1, 0, -1));
@@ -1130,61 +1170,72 @@ __global__ void k3_filter(D3 d, const double *in, double *out)
     out[ID3(i, j, k)] = filt(d, in, i, j, k);
 }
 
-__global__ void k3_magh(D3 d)
+// Germano-identity terms of the six components 11, 22, 33, 12, 13, 23
+// (stress_tensor_dy.f90:266-483) accumulated into LM and MM in that order, the
+// off-diagonal ones with weight 2; the strain rate of the filtered velocity and
+// its magnitude are formed once per cell (MAGH is kept for the heat flux).
+__global__ void k3_germano6(D3 d)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
-    double S[9], G[3];
-    strain3(d, d.UH, d.VH, d.WH, nullptr, i, j, k, S, G);
-    d.MAGH[ID3(i, j, k)] = sqrt(2.0 * sq9(S));
-}
-
-// Germano-identity terms of component q (11, 22, 33, 12, 13, 23), accumulated in
-// LM and MM (stress_tensor_dy.f90:266-483).
-__global__ void k3_germano(D3 d, int q)
-{
-    CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
-    const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
-    const int a = pa[q], b = pb[q], c = ID3(i, j, k);
+    const int c = ID3(i, j, k);
     const double *uf[3] = {d.U, d.V, d.W}, *uh[3] = {d.UH, d.VH, d.WH};
-    const double l = (-filt2(d, uf[a], uf[b], i, j, k)) + uh[a][c] * uh[b][c];
-    const double dout = filt2(d, d.MAG, d.L[3 * a + b], i, j, k);
     double S[9], G[3];
     strain3(d, d.UH, d.VH, d.WH, nullptr, i, j, k, S, G);
-    const double fac = a == b ? 0.5 : 0.25;
-    const double hs = S[3 * a + b] / fac;
-    double m = ((4.0 * d.MAGH[c]) * fac) * hs;
-    m = (d.FW[c] * d.FW[c]) * (m - dout);
-    if (q == 0) {
-        d.LM[c] = l * m;
-        d.MM[c] = m * m;
-    } else if (q < 3) {
-        d.LM[c] = d.LM[c] + l * m;
-        d.MM[c] = d.MM[c] + m * m;
-    } else {
-        d.LM[c] = d.LM[c] + (2.0 * l) * m;
-        d.MM[c] = d.MM[c] + (2.0 * m) * m;
+    const double magh = sqrt(2.0 * sq9(S));
+    d.MAGH[c] = magh;
+    const double fw2 = d.FW[c] * d.FW[c];
+    double lm = 0.0, mm = 0.0;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const int a = q < 3 ? q : (q == 5 ? 1 : 0), b = q < 3 ? q : (q == 3 ? 1 : 2);
+        const double l = (-filt2(d, uf[a], uf[b], i, j, k)) + uh[a][c] * uh[b][c];
+        const double dout = filt2(d, d.MAG, d.L[3 * a + b], i, j, k);
+        const double fac = a == b ? 0.5 : 0.25;
+        const double hs = S[3 * a + b] / fac;
+        double m = ((4.0 * magh) * fac) * hs;
+        m = fw2 * (m - dout);
+        if (q == 0) {
+            lm = l * m;
+            mm = m * m;
+        } else if (q < 3) {
+            lm = lm + l * m;
+            mm = mm + m * m;
+        } else {
+            lm = lm + (2.0 * l) * m;
+            mm = mm + (2.0 * m) * m;
+        }
     }
+    d.LM[c] = lm;
+    d.MM[c] = mm;
 }
 
-// Temperature terms P_q, R_q (stress_tensor_dy.f90:590-680)
-__global__ void k3_germano_t(D3 d, int q)
+// Temperature terms P_q, R_q of the three heat-flux components
+// (stress_tensor_dy.f90:590-680) accumulated into LM and MM.
+__global__ void k3_germano_t3(D3 d)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *uf[3] = {d.U, d.V, d.W}, *uh[3] = {d.UH, d.VH, d.WH};
     const double *M1[3] = {d.XIX, d.XIY, d.XIZ}, *M2[3] = {d.ETX, d.ETY, d.ETZ}, *M3[3] = {d.ZTX, d.ZTY, d.ZTZ};
-    const double l = (-filt2(d, uf[q], d.T, i, j, k)) + uh[q][c] * d.TH[c];
-    const double dout = filt2(d, d.MAG, d.DTD[q], i, j, k);
-    const double g = (dxi(d, M1[q], d.TH, i, j, k) + deta(d, M2[q], d.TH, i, j, k)) + dzeta(d, M3[q], d.TH, i, j, k);
-    double m = ((4.0 * d.MAGH[c]) * 0.5) * g;
-    m = (d.FW[c] * d.FW[c]) * (m - dout);
-    if (q == 0) {
-        d.LM[c] = l * m;
-        d.MM[c] = m * m;
-    } else {
-        d.LM[c] = d.LM[c] + l * m;
-        d.MM[c] = d.MM[c] + m * m;
+    const double fw2 = d.FW[c] * d.FW[c], magh = d.MAGH[c];
+    double lm = 0.0, mm = 0.0;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const double l = (-filt2(d, uf[q], d.T, i, j, k)) + uh[q][c] * d.TH[c];
+        const double dout = filt2(d, d.MAG, d.DTD[q], i, j, k);
+        const double g = (dxi(d, M1[q], d.TH, i, j, k) + deta(d, M2[q], d.TH, i, j, k)) + dzeta(d, M3[q], d.TH, i, j, k);
+        double m = ((4.0 * magh) * 0.5) * g;
+        m = fw2 * (m - dout);
+        if (q == 0) {
+            lm = l * m;
+            mm = m * m;
+        } else {
+            lm = lm + l * m;
+            mm = mm + m * m;
+        }
     }
+    d.LM[c] = lm;
+    d.MM[c] = mm;
 }
 
 // Volume-averaged coefficient over the points whose local coefficient is >= 0
@@ -1283,15 +1334,26 @@ __global__ void k3_sgst(D3 d)
 // ---------------------------------------------------------------------------------
 // CALCCOEF (calccoef.f90:9-160)
 // ---------------------------------------------------------------------------------
-__global__ void k3_cfl(D3 d)
+// CFL maximum: the maximum of the block (exact, order-free) goes to one atomic.
+__global__ void __launch_bounds__(128) k3_cfl(D3 d)
 {
-    CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
-    const int c = ID3(i, j, k);
-    const double u = d.U[c], v = d.V[c], w = d.W[c];
-    const double l = d.dt * ((fabs((d.XIX[c] * u + d.XIY[c] * v) + d.XIZ[c] * w) +
-                              fabs((d.ETX[c] * u + d.ETY[c] * v) + d.ETZ[c] * w)) +
-                             fabs((d.ZTX[c] * u + d.ZTY[c] * v) + d.ZTZ[c] * w));
-    atomicMax(d.cflbits, (unsigned long long)__double_as_longlong(l));
+    __shared__ double sh[4];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    double l = 0.0;
+    if (i <= d.NI - 1) {
+        const int c = ID3(i, j, k);
+        const double u = d.U[c], v = d.V[c], w = d.W[c];
+        l = d.dt * ((fabs((d.XIX[c] * u + d.XIY[c] * v) + d.XIZ[c] * w) +
+                     fabs((d.ETX[c] * u + d.ETY[c] * v) + d.ETZ[c] * w)) +
+                    fabs((d.ZTX[c] * u + d.ZTY[c] * v) + d.ZTZ[c] * w));
+    }
+    for (int o = 16; o > 0; o >>= 1) l = fmax(l, __shfl_xor_sync(0xffffffffu, l, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double m = fmax(fmax(sh[0], sh[1]), fmax(sh[2], sh[3]));
+        atomicMax(d.cflbits, (unsigned long long)__double_as_longlong(m));
+    }
 }
 
 // Wall force and heat-flux contributions of the two triangles of each wall face.
@@ -1326,9 +1388,39 @@ __global__ void k3_wall(D3 d)
     o[4] = ((d.T[c] - d.t_wall) / dn) * area;
 }
 
-// Fixed-order sums (the reference's loop order), coefficients into scal[3..14].
-__global__ void k3_calc_final(D3 d, double rtime, double sum_area)
+// Sums of the wall contributions in a fixed tree (one block: a strided partial sum
+// per thread, then the warps' shuffle trees, then the warps in order), the
+// coefficients into scal[3..16].
+__global__ void __launch_bounds__(1024) k3_calc_final(D3 d, double rtime, double sum_area)
 {
+    __shared__ double sh[5][32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int nj1 = d.NJ - 1, nk1 = d.NK - 1, plane = nj1 * nk1, total = 2 * plane;
+    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int e = t; e < total; e += blockDim.x) {
+        const int tri = e / plane, r = e - tri * plane, k = r / nj1 + 1, j = r - (k - 1) * nj1 + 1;
+        const double *o = d.wall + 8 * (size_t(tri) * d.NJ1 * (d.NK + 1) + JK(j, k));
+        acc[0] = acc[0] - o[0];
+        acc[1] = acc[1] - o[1];
+        acc[2] = acc[2] + o[2];
+        acc[3] = acc[3] + o[3];
+        acc[4] = acc[4] + o[4];
+    }
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+        if (lane == 0) sh[q][warp] = acc[q];
+    }
+    __syncthreads();
+    if (t != 0) return;
+    double pd = 0.0, pl = 0.0, td = 0.0, tl = 0.0, snu = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+        pd += sh[0][w];
+        pl += sh[1][w];
+        td += sh[2][w];
+        tl += sh[3][w];
+        snu += sh[4][w];
+    }
     const double *P = d.P;
     double dumb = 0.0;
     for (int k = 1; k <= d.NK - 1; k++) {
@@ -1339,17 +1431,6 @@ __global__ void k3_calc_final(D3 d, double rtime, double sum_area)
         dumb = dumb + pg;
     }
     dumb = dumb / (double)(d.NK - 1);
-    double pd = 0.0, pl = 0.0, td = 0.0, tl = 0.0, snu = 0.0;
-    for (int tri = 0; tri < 2; tri++)
-        for (int k = 1; k <= d.NK - 1; k++)
-            for (int j = 1; j <= d.NJ - 1; j++) {
-                const double *o = d.wall + 8 * (size_t(tri) * d.NJ1 * (d.NK + 1) + JK(j, k));
-                pd = pd - o[0];
-                pl = pl - o[1];
-                td = td + o[2];
-                tl = tl + o[3];
-                snu = snu + o[4];
-            }
     double *s = d.scal + 3;
     s[0] = rtime;
     s[1] = __longlong_as_double((long long)*d.cflbits);
@@ -1432,7 +1513,8 @@ void carve(Bump &b, fvm3_ctx *c)
     D3 &d = c->d;
     const size_t n = c->n, jk = size_t(c->NJ + 1) * (c->NK + 1);
     double **full[] = {&d.XG, &d.YG, &d.ZG, &d.X, &d.Y, &d.Z, &d.XIX, &d.XIY, &d.XIZ, &d.ETX, &d.ETY, &d.ETZ,
-                       &d.ZTX, &d.ZTY, &d.ZTZ, &d.DJAC, &d.Q11, &d.Q12, &d.Q13, &d.Q22, &d.Q23, &d.Q33, &d.DE,
+                       &d.ZTX, &d.ZTY, &d.ZTZ, &d.DJAC, &d.Q11, &d.Q12, &d.Q13, &d.Q22, &d.Q23, &d.Q33,
+                       &d.JQ12, &d.JQ13, &d.JQ23, &d.DE,
                        &d.DW, &d.DN, &d.DS, &d.DT, &d.DB, &d.THETA, &d.AREA1, &d.AREA2, &d.FW, &d.U, &d.V, &d.W,
                        &d.P, &d.T, &d.U_N, &d.V_N, &d.W_N, &d.T_N, &d.NLX, &d.NLY, &d.NLZ, &d.ADV, &d.NLX_NM1,
                        &d.NLY_NM1, &d.NLZ_NM1, &d.ADV_NM1, &d.DIFX, &d.DIFY, &d.DIFZ, &d.DIFT, &d.S_U, &d.S_V,
@@ -1480,7 +1562,7 @@ void carve(Bump &b, fvm3_ctx *c)
     }
     float **f32[] = {&d.RF, &d.DF, &d.ANf, &d.ASf, &d.ATf, &d.ABf};
     for (auto p : f32) *p = reinterpret_cast<float *>(b.take((n + 1) / 2));
-    d.nblk = 2 * 152;
+    d.nblk = 8 * 152;   // residual and reduction kernels: 8 blocks of 256 threads per SM
     d.partial = b.take(4 * size_t(d.nblk));
     d.pctl = reinterpret_cast<PCtl *>(b.take(8));
     d.scal = b.take(32);
@@ -1488,7 +1570,9 @@ void carve(Bump &b, fvm3_ctx *c)
     d.wall = b.take(16 * jk);
 }
 
-inline dim3 g_int(const fvm3_ctx *c) { return dim3((c->NI - 1 + 127) / 128, c->NJ - 1, c->NK - 1); }
+// Interior launches: 32 x 4 blocks in (I, J), one K plane per grid z.
+inline dim3 g_int(const fvm3_ctx *c) { return dim3((c->NI - 1 + 31) / 32, (c->NJ - 1 + 3) / 4, c->NK - 1); }
+const dim3 B_INT(32, 4, 1);
 inline dim3 g_full3(const fvm3_ctx *c) { return dim3((c->NI + 1 + 127) / 128, c->NJ + 1, c->NK + 1); }
 inline int g_lin(const fvm3_ctx *c) { return (c->n + 255) / 256; }
 
@@ -1559,14 +1643,14 @@ int setup_grid(fvm3_ctx *c)
     F3RC(halo(c, {d.MD[0], d.MD[1], d.MD[2], d.MD[3], d.MD[4], d.MD[5], d.MD[6], d.MD[7], d.MD[8]}));
     k3_jacobian<<<g_lin(c), 256, 0, st>>>(d);
     k3_q<<<g_lin(c), 256, 0, st>>>(d);
-    k3_dcoef<<<g_int(c), 128, 0, st>>>(d);
+    k3_dcoef<<<g_int(c), B_INT, 0, st>>>(d);
     k3_theta<<<g_lin(c), 256, 0, st>>>(d);
     k3_areas<<<dim3((c->NJ + 127) / 128, c->NK - 1), 128, 0, st>>>(d);
     for (int s = 0; s < 3; s++) {
-        k3_coef_af<<<g_int(c), 128, 0, st>>>(d, d.cf[s], s, d.re);
-        k3_coef_af<<<g_int(c), 128, 0, st>>>(d, d.cf[3 + s], s, d.pe);
+        k3_coef_af<<<g_int(c), B_INT, 0, st>>>(d, d.cf[s], s, d.re);
+        k3_coef_af<<<g_int(c), B_INT, 0, st>>>(d, d.cf[3 + s], s, d.pe);
     }
-    k3_coef_p<<<g_int(c), 128, 0, st>>>(d, d.cf[6]);
+    k3_coef_p<<<g_int(c), B_INT, 0, st>>>(d, d.cf[6]);
     k3_coef_f32<<<g_lin(c), 256, 0, st>>>(d);
     F3CHECK(c);
     for (int s = 0; s < 7; s++) {
@@ -1603,7 +1687,7 @@ int predictor(fvm3_ctx *c, int kind, double *phi, const double *phin, const doub
     D3 &d = c->d;
     const int base = kind == 2 ? 3 : 0;
     for (int split = 0; split < 3; split++) {
-        k3_af_rhs<<<g_int(c), 128, 0, c->stream>>>(d, d.cf[base + split], split, kind, phi, phin, ina, inb, inc, ind, ff);
+        k3_af_rhs<<<g_int(c), B_INT, 0, c->stream>>>(d, d.cf[base + split], split, kind, phi, phin, ina, inb, inc, ind, ff);
         k3_ghost<<<dim3((c->NJ + 1 + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, phi, ff, kind);
         F3RC(halo(c, {phi}));
         F3RC(line(c, base + split, d.SU, phi, 0));
@@ -1636,13 +1720,13 @@ int poisson_graph(fvm3_ctx *c)
             rc = line32(c, 0, 1);
             if (rc == FVM_OK) rc = line32(c, 1, 1);
         }
-        k3_apply<<<g_int(c), 128, 0, c->stream>>>(d);
+        k3_apply<<<g_int(c), B_INT, 0, c->stream>>>(d);
         k3_bcp<<<dim3((c->NJ + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, 1);
         if (rc == FVM_OK) rc = halo(c, {d.P});
     }
     for (int q = 0; q < groups && rc == FVM_OK && !mixed; q++) {
         for (int it = 0; it < per && rc == FVM_OK; it++) {
-            k3_psu<<<g_int(c), 128, 0, c->stream>>>(d);
+            k3_psu<<<g_int(c), B_INT, 0, c->stream>>>(d);
             k3_bcp<<<dim3((c->NJ + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, 1);
             rc = halo(c, {d.P});
             if (rc == FVM_OK) rc = line(c, 6, d.SU, d.P, 0, d.pctl);
@@ -1693,26 +1777,25 @@ int sgs(fvm3_ctx *c)
     F3RC(halo(c, {d.L[0], d.L[1], d.L[2], d.L[3], d.L[4], d.L[5], d.L[6], d.L[7], d.L[8], d.DTD[0], d.DTD[1],
                   d.DTD[2]}));
     k3_mag<<<g_lin(c), 256, 0, st>>>(d);
-    k3_filter<<<g_int(c), 128, 0, st>>>(d, d.U, d.UH);
-    k3_filter<<<g_int(c), 128, 0, st>>>(d, d.V, d.VH);
-    k3_filter<<<g_int(c), 128, 0, st>>>(d, d.W, d.WH);
-    k3_filter<<<g_int(c), 128, 0, st>>>(d, d.T, d.TH);
+    k3_filter<<<g_int(c), B_INT, 0, st>>>(d, d.U, d.UH);
+    k3_filter<<<g_int(c), B_INT, 0, st>>>(d, d.V, d.VH);
+    k3_filter<<<g_int(c), B_INT, 0, st>>>(d, d.W, d.WH);
+    k3_filter<<<g_int(c), B_INT, 0, st>>>(d, d.T, d.TH);
     F3RC(bcu(c, d.UH, d.FFU, 0));
     F3RC(bcu(c, d.VH, d.FFV, 1));
     F3RC(bcu(c, d.WH, d.FFW, 1));
     F3RC(bcu(c, d.TH, d.FFT, 2));
-    k3_magh<<<g_int(c), 128, 0, st>>>(d);
-    for (int q = 0; q < 6; q++) k3_germano<<<g_int(c), 128, 0, st>>>(d, q);
+    k3_germano6<<<g_int(c), B_INT, 0, st>>>(d);
     if (d.les_zavg) k3_czavg<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1), 128, 0, st>>>(d);
     else k3_cvol<<<d.nblk, 256, 0, st>>>(d, 0);
     k3_eddy<<<g_lin(c), 256, 0, st>>>(d, 0, d.EV);
-    k3_sgs<<<g_int(c), 128, 0, st>>>(d);
+    k3_sgs<<<g_int(c), B_INT, 0, st>>>(d);
     if (d.thermal) {
-        for (int q = 0; q < 3; q++) k3_germano_t<<<g_int(c), 128, 0, st>>>(d, q);
+        k3_germano_t3<<<g_int(c), B_INT, 0, st>>>(d);
         if (d.les_zavg) k3_czavg<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1), 128, 0, st>>>(d);
         else k3_cvol<<<d.nblk, 256, 0, st>>>(d, 1);
         k3_eddy<<<g_lin(c), 256, 0, st>>>(d, 1, d.EC);
-        k3_sgst<<<g_int(c), 128, 0, st>>>(d);
+        k3_sgst<<<g_int(c), B_INT, 0, st>>>(d);
     }
     F3CHECK(c);
     return FVM_OK;
@@ -1746,29 +1829,29 @@ int step(fvm3_ctx *c)
     k3_farfield<<<dim3((c->NJ + 127) / 128, c->NK - 1), 128, 0, st>>>(d);
     k3_contra<<<g_lin(c), 256, 0, st>>>(d);
     F3RC(halo(c, {d.U1, d.U2, d.U3}));
-    k3_fluxes<<<g_int(c), 128, 0, st>>>(d, 0);
-    k3_explicit<<<g_int(c), 128, 0, st>>>(d, d.thermal);
+    k3_fluxes<<<g_int(c), B_INT, 0, st>>>(d, 0);
+    k3_explicit<<<g_int(c), B_INT, 0, st>>>(d, d.thermal);
     F3CHECK(c);
     if (c->p.use_les) F3RC(sgs(c));
-    k3_dif<<<g_int(c), 128, 0, st>>>(d, d.thermal);
-    k3_psource<<<g_int(c), 128, 0, st>>>(d);
+    k3_dif<<<g_int(c), B_INT, 0, st>>>(d, d.thermal);
+    k3_psource<<<g_int(c), B_INT, 0, st>>>(d);
     F3CHECK(c);
     F3RC(predictor(c, 0, d.U, d.U_N, d.NLX, d.NLX_NM1, d.DIFX, d.S_U, d.FFU));
     F3RC(predictor(c, 1, d.V, d.V_N, d.NLY, d.NLY_NM1, d.DIFY, d.S_V, d.FFV));
     F3RC(predictor(c, 1, d.W, d.W_N, d.NLZ, d.NLZ_NM1, d.DIFZ, d.S_W, d.FFW));
-    k3_grad<<<g_int(c), 128, 0, st>>>(d, -1.0);
+    k3_grad<<<g_int(c), B_INT, 0, st>>>(d, -1.0);
     F3RC(bcu(c, d.U, d.FFU, 0));
     F3RC(bcu(c, d.V, d.FFV, 1));
     F3RC(bcu(c, d.W, d.FFW, 1));
     k3_contra<<<g_lin(c), 256, 0, st>>>(d);
     F3RC(halo(c, {d.U1, d.U2, d.U3}));
-    k3_fluxes<<<g_int(c), 128, 0, st>>>(d, 1);
+    k3_fluxes<<<g_int(c), B_INT, 0, st>>>(d, 1);
     F3CHECK(c);
     F3RC(poisson(c));
     k3_bcp<<<dim3((c->NJ + 127) / 128, c->NK + 1), 128, 0, st>>>(d, 0);
     F3RC(halo(c, {d.P}));
-    k3_psource<<<g_int(c), 128, 0, st>>>(d);
-    k3_grad<<<g_int(c), 128, 0, st>>>(d, +1.0);
+    k3_psource<<<g_int(c), B_INT, 0, st>>>(d);
+    k3_grad<<<g_int(c), B_INT, 0, st>>>(d, +1.0);
     k3_pref<<<1, 32, 0, st>>>(d);
     k3_pshift<<<g_lin(c), 256, 0, st>>>(d);
     F3RC(bcu(c, d.U, d.FFU, 0));
@@ -1778,9 +1861,9 @@ int step(fvm3_ctx *c)
         F3RC(predictor(c, 2, d.T, d.T_N, d.ADV, d.ADV_NM1, d.DIFT, nullptr, d.FFT));
         F3RC(bcu(c, d.T, d.FFT, 2));
     }
-    k3_cfl<<<g_int(c), 128, 0, st>>>(d);
+    k3_cfl<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1, c->NK - 1), 128, 0, st>>>(d);
     k3_wall<<<dim3((c->NJ + 127) / 128, c->NK - 1, 2), 128, 0, st>>>(d);
-    k3_calc_final<<<1, 1, 0, st>>>(d, c->rtime, c->sum_area);
+    k3_calc_final<<<1, 1024, 0, st>>>(d, c->rtime, c->sum_area);
     F3CHECK(c);
     return FVM_OK;
 }

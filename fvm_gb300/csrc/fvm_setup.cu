@@ -255,12 +255,10 @@ __global__ void k_dcoef(Dev d)
     d.PJDT[c] = (2.0 * d.pe) * J[c] / d.dt;
     if (i < 1 || i > d.NI - 1 || j < 1 || j > d.NJ - 1) return;
     {   // diagonal weights of the cross term 0.25*(Ke(fne-fse) - Kw(fnw-fsw) + Kn(fne-fnw) - Ks(fse-fsw))
-        const double *K = d.JQ12;
         double ke = __dmul_rn(J[IDX(i + 1, j)], d.Q12[IDX(i + 1, j)]);
         double kw = __dmul_rn(J[IDX(i - 1, j)], d.Q12[IDX(i - 1, j)]);
         double kn = __dmul_rn(J[IDX(i, j + 1)], d.Q12[IDX(i, j + 1)]);
         double ks = __dmul_rn(J[IDX(i, j - 1)], d.Q12[IDX(i, j - 1)]);
-        (void)K;
         d.CNE[c] = 0.25 * (ke + kn);
         d.CSE[c] = -(0.25 * (ke + ks));
         d.CNW[c] = -(0.25 * (kw + kn));
