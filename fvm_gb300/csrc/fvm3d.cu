@@ -1044,26 +1044,34 @@ namespace f3 {
 // ---------------------------------------------------------------------------------
 // Dynamic Smagorinsky model (stress_tensor_dy.f90:20-735, test_filter.f90:13-21)
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ double dxi(const D3 &d, const double *m, const double *f, int i, int j, int k)
+// The model's stencils are templates over the arithmetic type T: double for the
+// FP64 path; float for the mixed path, where the filters, the filtered strain and
+// the Germano terms run in FP32 on FP64 inputs (GB300's FP64 rate makes the 27-point
+// product filters ALU-bound in FP64) and the results are stored in FP64.
+template <class T>
+__device__ __forceinline__ T dxi(const D3 &d, const double *m, const double *f, int i, int j, int k)
 {
     const int c = ID3(i, j, k);
-    if (i == 0) return (2.0 * m[c]) * (f[ID3(1, j, k)] - f[c]);
-    if (i == d.NI) return (2.0 * m[c]) * (f[c] - f[ID3(d.NI - 1, j, k)]);
-    return m[c] * (f[ID3(i + 1, j, k)] - f[ID3(i - 1, j, k)]);
+    if (i == 0) return (T(2) * T(m[c])) * (T(f[ID3(1, j, k)]) - T(f[c]));
+    if (i == d.NI) return (T(2) * T(m[c])) * (T(f[c]) - T(f[ID3(d.NI - 1, j, k)]));
+    return T(m[c]) * (T(f[ID3(i + 1, j, k)]) - T(f[ID3(i - 1, j, k)]));
 }
-__device__ __forceinline__ double deta(const D3 &d, const double *m, const double *f, int i, int j, int k)
+template <class T>
+__device__ __forceinline__ T deta(const D3 &d, const double *m, const double *f, int i, int j, int k)
 {
-    return m[ID3(i, j, k)] * (f[ID3(i, j + 1, k)] - f[ID3(i, j - 1, k)]);
+    return T(m[ID3(i, j, k)]) * (T(f[ID3(i, j + 1, k)]) - T(f[ID3(i, j - 1, k)]));
 }
-__device__ __forceinline__ double dzeta(const D3 &d, const double *m, const double *f, int i, int j, int k)
+template <class T>
+__device__ __forceinline__ T dzeta(const D3 &d, const double *m, const double *f, int i, int j, int k)
 {
-    return m[ID3(i, j, k)] * (f[ID3(i, j, k + 1)] - f[ID3(i, j, k - 1)]);
+    return T(m[ID3(i, j, k)]) * (T(f[ID3(i, j, k + 1)]) - T(f[ID3(i, j, k - 1)]));
 }
 
 // Strain-rate components S11..S33 of (u,v,w) (0.5 / 0.25 times the index-difference
 // sums) and, with t, the temperature gradient (0.5 times the sums).
+template <class T>
 __device__ void strain3(const D3 &d, const double *u, const double *v, const double *w, const double *t, int i, int j,
-                        int k, double *S, double *G)
+                        int k, T *S, T *G)
 {
     const double *M1[3] = {d.XIX, d.XIY, d.XIZ}, *M2[3] = {d.ETX, d.ETY, d.ETZ}, *M3[3] = {d.ZTX, d.ZTY, d.ZTZ};
     const double *F[3] = {u, v, w};
@@ -1071,17 +1079,18 @@ __device__ void strain3(const D3 &d, const double *u, const double *v, const dou
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int b = a; b < 3; b++) {
-            double val;
+            T val;
             if (a == b) {
-                val = 0.5 * ((dxi(d, M1[a], F[a], i, j, k) + deta(d, M2[a], F[a], i, j, k)) + dzeta(d, M3[a], F[a], i, j, k));
+                val = T(0.5) * ((dxi<T>(d, M1[a], F[a], i, j, k) + deta<T>(d, M2[a], F[a], i, j, k)) +
+                                dzeta<T>(d, M3[a], F[a], i, j, k));
             } else {
-                double s = dxi(d, M1[b], F[a], i, j, k);
-                s = s + deta(d, M2[b], F[a], i, j, k);
-                s = s + dzeta(d, M3[b], F[a], i, j, k);
-                s = s + dxi(d, M1[a], F[b], i, j, k);
-                s = s + deta(d, M2[a], F[b], i, j, k);
-                s = s + dzeta(d, M3[a], F[b], i, j, k);
-                val = 0.25 * s;
+                T s = dxi<T>(d, M1[b], F[a], i, j, k);
+                s = s + deta<T>(d, M2[b], F[a], i, j, k);
+                s = s + dzeta<T>(d, M3[b], F[a], i, j, k);
+                s = s + dxi<T>(d, M1[a], F[b], i, j, k);
+                s = s + deta<T>(d, M2[a], F[b], i, j, k);
+                s = s + dzeta<T>(d, M3[a], F[b], i, j, k);
+                val = T(0.25) * s;
             }
             S[3 * a + b] = val;
             S[3 * b + a] = val;
@@ -1089,12 +1098,13 @@ __device__ void strain3(const D3 &d, const double *u, const double *v, const dou
     if (t)
 #pragma unroll
         for (int q = 0; q < 3; q++)
-            G[q] = 0.5 * ((dxi(d, M1[q], t, i, j, k) + deta(d, M2[q], t, i, j, k)) + dzeta(d, M3[q], t, i, j, k));
+            G[q] = T(0.5) * ((dxi<T>(d, M1[q], t, i, j, k) + deta<T>(d, M2[q], t, i, j, k)) + dzeta<T>(d, M3[q], t, i, j, k));
 }
 
-__device__ __forceinline__ double sq9(const double *S)
+template <class T>
+__device__ __forceinline__ T sq9(const T *S)
 {
-    double s = S[0] * S[0];
+    T s = S[0] * S[0];
 #pragma unroll
     for (int q = 1; q < 9; q++) s = s + S[q] * S[q];
     return s;
@@ -1104,7 +1114,7 @@ __global__ void k3_strain(D3 d)
 {
     CELL3(0, d.NI, 1, d.NJ - 1, 1, d.NK - 1)
     double S[9], G[3];
-    strain3(d, d.U, d.V, d.W, d.T, i, j, k, S, G);
+    strain3<double>(d, d.U, d.V, d.W, d.T, i, j, k, S, G);
     const int c = ID3(i, j, k);
 #pragma unroll
     for (int q = 0; q < 9; q++) d.L[q][c] = S[q];
@@ -1124,9 +1134,10 @@ __global__ void k3_mag(D3 d)
 
 // [1,2,1]^3 / 64 over the 27 neighbours of an interior cell, the reference's term
 // order (K-1 plane first, I fastest).
-__device__ __forceinline__ double filt(const D3 &d, const double *in, int i, int j, int k)
+template <class T>
+__device__ __forceinline__ T filt(const D3 &d, const double *in, int i, int j, int k)
 {
-    double s = 0.0;
+    T s = T(0);
     bool first = true;
 #pragma unroll
     for (int c = -1; c <= 1; c++)
@@ -1134,19 +1145,20 @@ __device__ __forceinline__ double filt(const D3 &d, const double *in, int i, int
         for (int b = -1; b <= 1; b++)
 #pragma unroll
             for (int a = -1; a <= 1; a++) {
-                const double wt = (double)((2 - (a * a)) * (2 - (b * b)) * (2 - (c * c)));
-                const double v = in[ID3(i + a, j + b, k + c)];
-                const double term = wt == 1.0 ? v : wt * v;
+                const T wt = T((2 - (a * a)) * (2 - (b * b)) * (2 - (c * c)));
+                const T v = T(in[ID3(i + a, j + b, k + c)]);
+                const T term = wt == T(1) ? v : wt * v;
                 s = first ? term : s + term;
                 first = false;
             }
-    return s / 64.0;
+    return s / T(64);
 }
 
 // product-filter: filt(f*g) with the product formed per neighbour
-__device__ __forceinline__ double filt2(const D3 &d, const double *f, const double *g, int i, int j, int k)
+template <class T>
+__device__ __forceinline__ T filt2(const D3 &d, const double *f, const double *g, int i, int j, int k)
 {
-    double s = 0.0;
+    T s = T(0);
     bool first = true;
 #pragma unroll
     for (int c = -1; c <= 1; c++)
@@ -1154,45 +1166,47 @@ __device__ __forceinline__ double filt2(const D3 &d, const double *f, const doub
         for (int b = -1; b <= 1; b++)
 #pragma unroll
             for (int a = -1; a <= 1; a++) {
-                const double wt = (double)((2 - (a * a)) * (2 - (b * b)) * (2 - (c * c)));
+                const T wt = T((2 - (a * a)) * (2 - (b * b)) * (2 - (c * c)));
                 const int q = ID3(i + a, j + b, k + c);
-                const double v = f[q] * g[q];
-                const double term = wt == 1.0 ? v : wt * v;
+                const T v = T(f[q]) * T(g[q]);
+                const T term = wt == T(1) ? v : wt * v;
                 s = first ? term : s + term;
                 first = false;
             }
-    return s / 64.0;
+    return s / T(64);
 }
 
+template <class T>
 __global__ void k3_filter(D3 d, const double *in, double *out)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
-    out[ID3(i, j, k)] = filt(d, in, i, j, k);
+    out[ID3(i, j, k)] = (double)filt<T>(d, in, i, j, k);
 }
 
 // Germano-identity terms of the six components 11, 22, 33, 12, 13, 23
 // (stress_tensor_dy.f90:266-483) accumulated into LM and MM in that order, the
 // off-diagonal ones with weight 2; the strain rate of the filtered velocity and
 // its magnitude are formed once per cell (MAGH is kept for the heat flux).
+template <class T>
 __global__ void k3_germano6(D3 d)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *uf[3] = {d.U, d.V, d.W}, *uh[3] = {d.UH, d.VH, d.WH};
-    double S[9], G[3];
-    strain3(d, d.UH, d.VH, d.WH, nullptr, i, j, k, S, G);
-    const double magh = sqrt(2.0 * sq9(S));
-    d.MAGH[c] = magh;
-    const double fw2 = d.FW[c] * d.FW[c];
-    double lm = 0.0, mm = 0.0;
+    T S[9], G[3];
+    strain3<T>(d, d.UH, d.VH, d.WH, nullptr, i, j, k, S, G);
+    const T magh = sqrt(T(2) * sq9<T>(S));
+    d.MAGH[c] = (double)magh;
+    const T fw2 = T(d.FW[c]) * T(d.FW[c]);
+    T lm = T(0), mm = T(0);
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         const int a = q < 3 ? q : (q == 5 ? 1 : 0), b = q < 3 ? q : (q == 3 ? 1 : 2);
-        const double l = (-filt2(d, uf[a], uf[b], i, j, k)) + uh[a][c] * uh[b][c];
-        const double dout = filt2(d, d.MAG, d.L[3 * a + b], i, j, k);
-        const double fac = a == b ? 0.5 : 0.25;
-        const double hs = S[3 * a + b] / fac;
-        double m = ((4.0 * magh) * fac) * hs;
+        const T l = (-filt2<T>(d, uf[a], uf[b], i, j, k)) + T(uh[a][c]) * T(uh[b][c]);
+        const T dout = filt2<T>(d, d.MAG, d.L[3 * a + b], i, j, k);
+        const T fac = a == b ? T(0.5) : T(0.25);
+        const T hs = S[3 * a + b] / fac;
+        T m = ((T(4) * magh) * fac) * hs;
         m = fw2 * (m - dout);
         if (q == 0) {
             lm = l * m;
@@ -1201,30 +1215,32 @@ __global__ void k3_germano6(D3 d)
             lm = lm + l * m;
             mm = mm + m * m;
         } else {
-            lm = lm + (2.0 * l) * m;
-            mm = mm + (2.0 * m) * m;
+            lm = lm + (T(2) * l) * m;
+            mm = mm + (T(2) * m) * m;
         }
     }
-    d.LM[c] = lm;
-    d.MM[c] = mm;
+    d.LM[c] = (double)lm;
+    d.MM[c] = (double)mm;
 }
 
 // Temperature terms P_q, R_q of the three heat-flux components
 // (stress_tensor_dy.f90:590-680) accumulated into LM and MM.
+template <class T>
 __global__ void k3_germano_t3(D3 d)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *uf[3] = {d.U, d.V, d.W}, *uh[3] = {d.UH, d.VH, d.WH};
     const double *M1[3] = {d.XIX, d.XIY, d.XIZ}, *M2[3] = {d.ETX, d.ETY, d.ETZ}, *M3[3] = {d.ZTX, d.ZTY, d.ZTZ};
-    const double fw2 = d.FW[c] * d.FW[c], magh = d.MAGH[c];
-    double lm = 0.0, mm = 0.0;
+    const T fw2 = T(d.FW[c]) * T(d.FW[c]), magh = T(d.MAGH[c]);
+    T lm = T(0), mm = T(0);
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        const double l = (-filt2(d, uf[q], d.T, i, j, k)) + uh[q][c] * d.TH[c];
-        const double dout = filt2(d, d.MAG, d.DTD[q], i, j, k);
-        const double g = (dxi(d, M1[q], d.TH, i, j, k) + deta(d, M2[q], d.TH, i, j, k)) + dzeta(d, M3[q], d.TH, i, j, k);
-        double m = ((4.0 * magh) * 0.5) * g;
+        const T l = (-filt2<T>(d, uf[q], d.T, i, j, k)) + T(uh[q][c]) * T(d.TH[c]);
+        const T dout = filt2<T>(d, d.MAG, d.DTD[q], i, j, k);
+        const T g = (dxi<T>(d, M1[q], d.TH, i, j, k) + deta<T>(d, M2[q], d.TH, i, j, k)) +
+                    dzeta<T>(d, M3[q], d.TH, i, j, k);
+        T m = ((T(4) * magh) * T(0.5)) * g;
         m = fw2 * (m - dout);
         if (q == 0) {
             lm = l * m;
@@ -1234,8 +1250,8 @@ __global__ void k3_germano_t3(D3 d)
             mm = mm + m * m;
         }
     }
-    d.LM[c] = lm;
-    d.MM[c] = mm;
+    d.LM[c] = (double)lm;
+    d.MM[c] = (double)mm;
 }
 
 // Volume-averaged coefficient over the points whose local coefficient is >= 0
@@ -1777,21 +1793,23 @@ int sgs(fvm3_ctx *c)
     F3RC(halo(c, {d.L[0], d.L[1], d.L[2], d.L[3], d.L[4], d.L[5], d.L[6], d.L[7], d.L[8], d.DTD[0], d.DTD[1],
                   d.DTD[2]}));
     k3_mag<<<g_lin(c), 256, 0, st>>>(d);
-    k3_filter<<<g_int(c), B_INT, 0, st>>>(d, d.U, d.UH);
-    k3_filter<<<g_int(c), B_INT, 0, st>>>(d, d.V, d.VH);
-    k3_filter<<<g_int(c), B_INT, 0, st>>>(d, d.W, d.WH);
-    k3_filter<<<g_int(c), B_INT, 0, st>>>(d, d.T, d.TH);
+    const bool f32 = c->p.precision == FVM_MIXED;   // the model's stencils in FP32
+    auto filter = f32 ? k3_filter<float> : k3_filter<double>;
+    filter<<<g_int(c), B_INT, 0, st>>>(d, d.U, d.UH);
+    filter<<<g_int(c), B_INT, 0, st>>>(d, d.V, d.VH);
+    filter<<<g_int(c), B_INT, 0, st>>>(d, d.W, d.WH);
+    filter<<<g_int(c), B_INT, 0, st>>>(d, d.T, d.TH);
     F3RC(bcu(c, d.UH, d.FFU, 0));
     F3RC(bcu(c, d.VH, d.FFV, 1));
     F3RC(bcu(c, d.WH, d.FFW, 1));
     F3RC(bcu(c, d.TH, d.FFT, 2));
-    k3_germano6<<<g_int(c), B_INT, 0, st>>>(d);
+    (f32 ? k3_germano6<float> : k3_germano6<double>)<<<g_int(c), B_INT, 0, st>>>(d);
     if (d.les_zavg) k3_czavg<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1), 128, 0, st>>>(d);
     else k3_cvol<<<d.nblk, 256, 0, st>>>(d, 0);
     k3_eddy<<<g_lin(c), 256, 0, st>>>(d, 0, d.EV);
     k3_sgs<<<g_int(c), B_INT, 0, st>>>(d);
     if (d.thermal) {
-        k3_germano_t3<<<g_int(c), B_INT, 0, st>>>(d);
+        (f32 ? k3_germano_t3<float> : k3_germano_t3<double>)<<<g_int(c), B_INT, 0, st>>>(d);
         if (d.les_zavg) k3_czavg<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1), 128, 0, st>>>(d);
         else k3_cvol<<<d.nblk, 256, 0, st>>>(d, 1);
         k3_eddy<<<g_lin(c), 256, 0, st>>>(d, 1, d.EC);
