@@ -8,8 +8,11 @@ import numpy as np
 
 from . import capi
 
+ROUTINES = ["fvm3_begin_step", "fvm3_contra_vel", "fvm3_nl", "fvm3_stress_tensor", "fvm3_dif", "fvm3_p_source",
+            "fvm3_remove_grad", "fvm3_correct", "fvm3_iter_t"]
 EXPORTS = ["fvm3_default_params", "fvm3_create", "fvm3_destroy", "fvm3_last_error", "fvm3_set_grid", "fvm3_init",
-           "fvm3_step", "fvm3_get_array", "fvm3_set_array", "fvm3_sgs", "fvm3_time_sweeps", "fvm3_get_stream"]
+           "fvm3_step", "fvm3_get_array", "fvm3_set_array", "fvm3_sgs", "fvm3_time_sweeps", "fvm3_get_stream",
+           "fvm3_iter_u", "fvm3_iter_p", "fvm3_calccoef", "fvm3_test_filter"] + ROUTINES
 
 
 class Params3(ctypes.Structure):
@@ -52,6 +55,12 @@ def load():
         L.fvm3_sgs.argtypes = [V, ctypes.POINTER(Coeffs3)]
         L.fvm3_time_sweeps.argtypes = [V, ctypes.c_int, D]
         L.fvm3_get_stream.argtypes = [V, ctypes.POINTER(V)]
+        for f in ROUTINES:
+            getattr(L, f).argtypes = [V]
+        L.fvm3_iter_u.argtypes = [V, ctypes.c_int]
+        L.fvm3_iter_p.argtypes = [V, D, ctypes.POINTER(ctypes.c_int)]
+        L.fvm3_calccoef.argtypes = [V, ctypes.POINTER(Coeffs3)]
+        L.fvm3_test_filter.argtypes = [V, D, D]
         _ready = True
     return L
 
@@ -121,6 +130,35 @@ class Context3:
         c = Coeffs3()
         self._ok(self.L.fvm3_step(self.h, n, ctypes.byref(c)), allow=(capi.FVM_ERR_NOCONV,))
         return c.as_dict()
+
+    def call(self, name):
+        """One per-routine call point without arguments, e.g. call("begin_step")."""
+        f = "fvm3_" + name
+        if f not in ROUTINES:
+            raise KeyError(name)
+        self._ok(getattr(self.L, f)(self.h))
+
+    def iter_u(self, component):
+        self._ok(self.L.fvm3_iter_u(self.h, component))
+
+    def iter_p(self):
+        """CONTRA_VEL, ITER_P, BCP; returns (scaled residual, sweeps)."""
+        r = ctypes.c_double()
+        n = ctypes.c_int()
+        self._ok(self.L.fvm3_iter_p(self.h, ctypes.byref(r), ctypes.byref(n)), allow=(capi.FVM_ERR_NOCONV,))
+        return r.value, n.value
+
+    def calccoef(self) -> dict:
+        c = Coeffs3()
+        self._ok(self.L.fvm3_calccoef(self.h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def test_filter(self, a, out=None) -> np.ndarray:
+        """TEST_FILTER(IN, OUT): the box filter of a into the interior of out."""
+        src = self._arr(a)
+        dst = np.zeros(self.n) if out is None else self._arr(out).copy()
+        self._ok(self.L.fvm3_test_filter(self.h, _dp(src), _dp(dst)))
+        return dst.reshape(self.shape)
 
     def sgs(self) -> dict:
         c = Coeffs3()

@@ -61,6 +61,8 @@ struct D3 {
     // MIXED Poisson: FP32 residual and correction, FP32 copies of the transverse
     // couplings of the Poisson set
     float *RF, *DF, *ANf, *ASf, *ATf, *ABf;
+    // SGS model: two banks of 12 arrays for the separable test filters
+    double *FB;
     // reductions
     PCtl *pctl;
     double *partial;        // 4 per block
@@ -642,35 +644,41 @@ __device__ __forceinline__ double nl3(const D3 &d, const double *in, int c, int 
                     d.WT[c] * (in[ID3(i, j, k + 1)] + p)) - d.WB[c] * (in[ID3(i, j, k - 1)] + p)));
 }
 
-// DIF_DIAGONAL (dif_diagonal.f90:13-32): twelve cross terms with Q*J
-__device__ __forceinline__ double cross12(const D3 &d, const double *f, int i, int j, int k)
+// DIF_DIAGONAL (dif_diagonal.f90:13-32): twelve cross terms with Q*J.  T is the
+// arithmetic type of the weighted sum (double, or float in the mixed path's DIF);
+// the differences of f are formed in FP64 first.
+template <class T = double>
+__device__ __forceinline__ T cross12(const D3 &d, const double *f, int i, int j, int k)
 {
 #define F3(a, b, c) f[ID3(i + (a), j + (b), k + (c))]
-#define G3(Q, a, b, c) (d.J##Q[ID3(i + (a), j + (b), k + (c))])
-    double s = G3(Q12, 1, 0, 0) * (F3(1, 1, 0) - F3(1, -1, 0));
-    s = s - G3(Q12, -1, 0, 0) * (F3(-1, 1, 0) - F3(-1, -1, 0));
-    s = s + G3(Q13, 1, 0, 0) * (F3(1, 0, 1) - F3(1, 0, -1));
-    s = s - G3(Q13, -1, 0, 0) * (F3(-1, 0, 1) - F3(-1, 0, -1));
-    s = s + G3(Q12, 0, 1, 0) * (F3(1, 1, 0) - F3(-1, 1, 0));
-    s = s - G3(Q12, 0, -1, 0) * (F3(1, -1, 0) - F3(-1, -1, 0));
-    s = s + G3(Q23, 0, 1, 0) * (F3(0, 1, 1) - F3(0, 1, -1));
-    s = s - G3(Q23, 0, -1, 0) * (F3(0, -1, 1) - F3(0, -1, -1));
-    s = s + G3(Q13, 0, 0, 1) * (F3(1, 0, 1) - F3(-1, 0, 1));
-    s = s - G3(Q13, 0, 0, -1) * (F3(1, 0, -1) - F3(-1, 0, -1));
-    s = s + G3(Q23, 0, 0, 1) * (F3(0, 1, 1) - F3(0, -1, 1));
-    s = s - G3(Q23, 0, 0, -1) * (F3(0, 1, -1) - F3(0, -1, -1));
+#define G3(Q, a, b, c) T(d.J##Q[ID3(i + (a), j + (b), k + (c))])
+#define DF(x) T(x)
+    T s = G3(Q12, 1, 0, 0) * DF(F3(1, 1, 0) - F3(1, -1, 0));
+    s = s - G3(Q12, -1, 0, 0) * DF(F3(-1, 1, 0) - F3(-1, -1, 0));
+    s = s + G3(Q13, 1, 0, 0) * DF(F3(1, 0, 1) - F3(1, 0, -1));
+    s = s - G3(Q13, -1, 0, 0) * DF(F3(-1, 0, 1) - F3(-1, 0, -1));
+    s = s + G3(Q12, 0, 1, 0) * DF(F3(1, 1, 0) - F3(-1, 1, 0));
+    s = s - G3(Q12, 0, -1, 0) * DF(F3(1, -1, 0) - F3(-1, -1, 0));
+    s = s + G3(Q23, 0, 1, 0) * DF(F3(0, 1, 1) - F3(0, 1, -1));
+    s = s - G3(Q23, 0, -1, 0) * DF(F3(0, -1, 1) - F3(0, -1, -1));
+    s = s + G3(Q13, 0, 0, 1) * DF(F3(1, 0, 1) - F3(-1, 0, 1));
+    s = s - G3(Q13, 0, 0, -1) * DF(F3(1, 0, -1) - F3(-1, 0, -1));
+    s = s + G3(Q23, 0, 0, 1) * DF(F3(0, 1, 1) - F3(0, -1, 1));
+    s = s - G3(Q23, 0, 0, -1) * DF(F3(0, 1, -1) - F3(0, -1, -1));
 #undef F3
 #undef G3
-    return 0.25 * s;
+#undef DF
+    return T(0.25) * s;
 }
 
+template <class T>
 __device__ __forceinline__ double dif3(const D3 &d, const double *in, int c, int i, int j, int k)
 {   // DIF (dif.f90:15-23)
     const double p = in[c];
-    return 1.0 * ((((((d.DE[c] * (in[ID3(i + 1, j, k)] - p) + d.DW[c] * (in[ID3(i - 1, j, k)] - p)) +
-                      d.DN[c] * (in[ID3(i, j + 1, k)] - p)) + d.DS[c] * (in[ID3(i, j - 1, k)] - p)) +
-                    d.DT[c] * (in[ID3(i, j, k + 1)] - p)) + d.DB[c] * (in[ID3(i, j, k - 1)] - p)) +
-                  cross12(d, in, i, j, k));
+    return (double)(T(1) * ((((((T(d.DE[c]) * T(in[ID3(i + 1, j, k)] - p) + T(d.DW[c]) * T(in[ID3(i - 1, j, k)] - p)) +
+                                T(d.DN[c]) * T(in[ID3(i, j + 1, k)] - p)) + T(d.DS[c]) * T(in[ID3(i, j - 1, k)] - p)) +
+                              T(d.DT[c]) * T(in[ID3(i, j, k + 1)] - p)) + T(d.DB[c]) * T(in[ID3(i, j, k - 1)] - p)) +
+                            cross12<T>(d, in, i, j, k)));
 }
 
 // NL of the four fields (shifting the previous values to *_NM1), DIF of the four
@@ -689,14 +697,17 @@ __global__ void k3_explicit(D3 d, int thermal)
     if (thermal) d.ADV[c] = nl3(d, d.T_N, c, i, j, k);
 }
 
+// DIF of the four fields; T = float in the mixed path (the stencil sums in FP32 on
+// FP64 differences, the result stored in FP64).
+template <class T>
 __global__ void k3_dif(D3 d, int thermal)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
-    d.DIFX[c] = dif3(d, d.U_N, c, i, j, k);
-    d.DIFY[c] = dif3(d, d.V_N, c, i, j, k);
-    d.DIFZ[c] = dif3(d, d.W_N, c, i, j, k);
-    if (thermal) d.DIFT[c] = dif3(d, d.T_N, c, i, j, k);
+    d.DIFX[c] = dif3<T>(d, d.U_N, c, i, j, k);
+    d.DIFY[c] = dif3<T>(d, d.V_N, c, i, j, k);
+    d.DIFZ[c] = dif3<T>(d, d.W_N, c, i, j, k);
+    if (thermal) d.DIFT[c] = dif3<T>(d, d.T_N, c, i, j, k);
 }
 
 __global__ void k3_psource(D3 d)
@@ -758,6 +769,9 @@ __global__ void k3_ghost(D3 d, double *phi, const double *ff, int kind)
 
 // Right-hand side of one AF sweep (iter_u.f90:44-100, iter_T.f90): the split's
 // twelve cross terms of phi, the sweep's source, and the BC folding of BCU/BCT.
+// T: arithmetic type of the cross terms (float in the mixed path, on FP64
+// differences); the source terms are always FP64.
+template <class T>
 __global__ void k3_af_rhs(D3 d, Coef3 cf, int split, int kind, const double *phi, const double *phin,
                           const double *ina, const double *inb, const double *inc, const double *ind,
                           const double *ff)
@@ -769,22 +783,22 @@ __global__ void k3_af_rhs(D3 d, Coef3 cf, int split, int kind, const double *phi
     const double *m2 = split == 0 ? d.ETX : (split == 1 ? d.ETY : d.ETZ);
     const double *m3 = split == 0 ? d.ZTX : (split == 1 ? d.ZTY : d.ZTZ);
 #define F3(a, b, cc) phi[ID3(i + (a), j + (b), k + (cc))]
-#define P3(ma, mb, a, b, cc) ((J[ID3(i + (a), j + (b), k + (cc))] * ma[ID3(i + (a), j + (b), k + (cc))]) * mb[ID3(i + (a), j + (b), k + (cc))])
-    double s = P3(m1, m2, 1, 0, 0) * (F3(1, 1, 0) - F3(1, -1, 0));
-    s = s - P3(m1, m2, -1, 0, 0) * (F3(-1, 1, 0) - F3(-1, -1, 0));
-    s = s + P3(m1, m3, 1, 0, 0) * (F3(1, 0, 1) - F3(1, 0, -1));
-    s = s - P3(m1, m3, -1, 0, 0) * (F3(-1, 0, 1) - F3(-1, 0, -1));
-    s = s + P3(m2, m1, 0, 1, 0) * (F3(1, 1, 0) - F3(-1, 1, 0));
-    s = s - P3(m2, m1, 0, -1, 0) * (F3(1, -1, 0) - F3(-1, -1, 0));
-    s = s + P3(m2, m3, 0, 1, 0) * (F3(0, 1, 1) - F3(0, 1, -1));
-    s = s - P3(m2, m3, 0, -1, 0) * (F3(0, -1, 1) - F3(0, -1, -1));
-    s = s + P3(m3, m1, 0, 0, 1) * (F3(1, 0, 1) - F3(-1, 0, 1));
-    s = s - P3(m3, m1, 0, 0, -1) * (F3(1, 0, -1) - F3(-1, 0, -1));
-    s = s + P3(m3, m2, 0, 0, 1) * (F3(0, 1, 1) - F3(0, -1, 1));
-    s = s - P3(m3, m2, 0, 0, -1) * (F3(0, 1, -1) - F3(0, -1, -1));
+#define P3(ma, mb, a, b, cc) ((T(J[ID3(i + (a), j + (b), k + (cc))]) * T(ma[ID3(i + (a), j + (b), k + (cc))])) * T(mb[ID3(i + (a), j + (b), k + (cc))]))
+    T s = P3(m1, m2, 1, 0, 0) * T(F3(1, 1, 0) - F3(1, -1, 0));
+    s = s - P3(m1, m2, -1, 0, 0) * T(F3(-1, 1, 0) - F3(-1, -1, 0));
+    s = s + P3(m1, m3, 1, 0, 0) * T(F3(1, 0, 1) - F3(1, 0, -1));
+    s = s - P3(m1, m3, -1, 0, 0) * T(F3(-1, 0, 1) - F3(-1, 0, -1));
+    s = s + P3(m2, m1, 0, 1, 0) * T(F3(1, 1, 0) - F3(-1, 1, 0));
+    s = s - P3(m2, m1, 0, -1, 0) * T(F3(1, -1, 0) - F3(-1, -1, 0));
+    s = s + P3(m2, m3, 0, 1, 0) * T(F3(0, 1, 1) - F3(0, 1, -1));
+    s = s - P3(m2, m3, 0, -1, 0) * T(F3(0, -1, 1) - F3(0, -1, -1));
+    s = s + P3(m3, m1, 0, 0, 1) * T(F3(1, 0, 1) - F3(-1, 0, 1));
+    s = s - P3(m3, m1, 0, 0, -1) * T(F3(1, 0, -1) - F3(-1, 0, -1));
+    s = s + P3(m3, m2, 0, 0, 1) * T(F3(0, 1, 1) - F3(0, -1, 1));
+    s = s - P3(m3, m2, 0, 0, -1) * T(F3(0, 1, -1) - F3(0, -1, -1));
 #undef F3
 #undef P3
-    const double dd = 0.25 * s;
+    const double dd = (double)(T(0.25) * s);
     const double rek = kind == 2 ? d.pe : d.re;
     const double r = ((2.0 * rek) * J[c]) / d.dt;
     double su;
@@ -1154,28 +1168,6 @@ __device__ __forceinline__ T filt(const D3 &d, const double *in, int i, int j, i
     return s / T(64);
 }
 
-// product-filter: filt(f*g) with the product formed per neighbour
-template <class T>
-__device__ __forceinline__ T filt2(const D3 &d, const double *f, const double *g, int i, int j, int k)
-{
-    T s = T(0);
-    bool first = true;
-#pragma unroll
-    for (int c = -1; c <= 1; c++)
-#pragma unroll
-        for (int b = -1; b <= 1; b++)
-#pragma unroll
-            for (int a = -1; a <= 1; a++) {
-                const T wt = T((2 - (a * a)) * (2 - (b * b)) * (2 - (c * c)));
-                const int q = ID3(i + a, j + b, k + c);
-                const T v = T(f[q]) * T(g[q]);
-                const T term = wt == T(1) ? v : wt * v;
-                s = first ? term : s + term;
-                first = false;
-            }
-    return s / T(64);
-}
-
 template <class T>
 __global__ void k3_filter(D3 d, const double *in, double *out)
 {
@@ -1183,30 +1175,95 @@ __global__ void k3_filter(D3 d, const double *in, double *out)
     out[ID3(i, j, k)] = (double)filt<T>(d, in, i, j, k);
 }
 
-// Germano-identity terms of the six components 11, 22, 33, 12, 13, 23
-// (stress_tensor_dy.f90:266-483) accumulated into LM and MM in that order, the
-// off-diagonal ones with weight 2; the strain rate of the filtered velocity and
-// its magnitude are formed once per cell (MAGH is kept for the heat flux).
-template <class T>
-__global__ void k3_germano6(D3 d)
+// ---------------------------------------------------------------------------------
+// The test filter (test_filter.f90:13-21) applied separably: the [1,2,1]^3/64 box
+// filter is the product of three [1,2,1] passes, I, J, then K with the 1/64, so
+// the 22 filters of a step (the filtered velocity and temperature, the Germano
+// products, the heat-flux products) read each input three times instead of 27.
+// Bank b, array q at FB + (12 b + q) n.  The result is the reference's 27-point
+// sum up to rounding (the terms are added in another order).
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double *fbank(const D3 &d, int b, int q) { return d.FB + (size_t(12 * b + q)) * d.n; }
+
+enum { SEP_HATS = 0, SEP_VEL = 1, SEP_HEAT = 2 };
+
+// Filter inputs over the whole array into bank 0: U, V, W, T (SEP_HATS); the
+// velocity products uu, vv, ww, uv, uw, vw and MAG*S11, S22, S33, S12, S13, S23
+// (SEP_VEL, stress_tensor_dy.f90:266-483); uT, vT, wT and MAG*dT/dx_q (SEP_HEAT,
+// stress_tensor_dy.f90:590-680).
+__global__ void k3_prod(D3 d, int mode)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    const double u = d.U[c], v = d.V[c], w = d.W[c], t = d.T[c], mg = d.MAG[c];
+    if (mode == SEP_HATS) {
+        fbank(d, 0, 0)[c] = u;
+        fbank(d, 0, 1)[c] = v;
+        fbank(d, 0, 2)[c] = w;
+        fbank(d, 0, 3)[c] = t;
+    } else if (mode == SEP_VEL) {
+        const double uv[3] = {u, v, w};
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            const int a = q < 3 ? q : (q == 5 ? 1 : 0), b = q < 3 ? q : (q == 3 ? 1 : 2);
+            fbank(d, 0, q)[c] = uv[a] * uv[b];
+            fbank(d, 0, 6 + q)[c] = mg * d.L[3 * a + b][c];
+        }
+    } else {
+        fbank(d, 0, 0)[c] = u * t;
+        fbank(d, 0, 1)[c] = v * t;
+        fbank(d, 0, 2)[c] = w * t;
+#pragma unroll
+        for (int q = 0; q < 3; q++) fbank(d, 0, 3 + q)[c] = mg * d.DTD[q][c];
+    }
+}
+
+struct Out4 {
+    double *p[4];
+};
+
+// One [1,2,1] pass over nq arrays from bank src to bank dst: dir 0 (I) for
+// i = 1..NI-1 on every (j, k); dir 1 (J) for j = 1..NJ-1 on every k; dir 2 (K) on
+// the interior, with the 1/64, into bank dst or, when out.p[0] is set, into out.p[q].
+__global__ void k3_sep(D3 d, int src, int dst, int nq, int dir, Out4 out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + (dir == 0 ? 0 : 1);
+    const int k = blockIdx.z + (dir == 2 ? 1 : 0);
+    if (i > d.NI - 1 || j > (dir == 0 ? d.NJ : d.NJ - 1) || k > (dir == 2 ? d.NK - 1 : d.NK)) return;
+    const int c = ID3(i, j, k), o = dir == 0 ? 1 : (dir == 1 ? d.NI1 : d.NI1 * d.NJ1);
+    for (int q = 0; q < nq; q++) {
+        const double *a = fbank(d, src, q);
+        const double r = (a[c - o] + 2.0 * a[c]) + a[c + o];
+        if (dir != 2) fbank(d, dst, q)[c] = r;
+        else if (out.p[0]) out.p[q][c] = r / 64.0;
+        else fbank(d, dst, q)[c] = r / 64.0;
+    }
+}
+
+// Germano terms of the six velocity components (11, 22, 33, 12, 13, 23) from the
+// filtered products in bank b, accumulated into LM and MM in that order with the
+// off-diagonal ones weighted 2; the strain rate of the filtered velocity and its
+// magnitude once per cell (MAGH is kept for the heat flux).
+__global__ void k3_germano(D3 d, int b)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
-    const double *uf[3] = {d.U, d.V, d.W}, *uh[3] = {d.UH, d.VH, d.WH};
-    T S[9], G[3];
-    strain3<T>(d, d.UH, d.VH, d.WH, nullptr, i, j, k, S, G);
-    const T magh = sqrt(T(2) * sq9<T>(S));
-    d.MAGH[c] = (double)magh;
-    const T fw2 = T(d.FW[c]) * T(d.FW[c]);
-    T lm = T(0), mm = T(0);
+    const double *uh[3] = {d.UH, d.VH, d.WH};
+    double S[9], G[3];
+    strain3<double>(d, d.UH, d.VH, d.WH, nullptr, i, j, k, S, G);
+    const double magh = sqrt(2.0 * sq9<double>(S));
+    d.MAGH[c] = magh;
+    const double fw2 = d.FW[c] * d.FW[c];
+    double lm = 0.0, mm = 0.0;
 #pragma unroll
     for (int q = 0; q < 6; q++) {
-        const int a = q < 3 ? q : (q == 5 ? 1 : 0), b = q < 3 ? q : (q == 3 ? 1 : 2);
-        const T l = (-filt2<T>(d, uf[a], uf[b], i, j, k)) + T(uh[a][c]) * T(uh[b][c]);
-        const T dout = filt2<T>(d, d.MAG, d.L[3 * a + b], i, j, k);
-        const T fac = a == b ? T(0.5) : T(0.25);
-        const T hs = S[3 * a + b] / fac;
-        T m = ((T(4) * magh) * fac) * hs;
+        const int a = q < 3 ? q : (q == 5 ? 1 : 0), bb = q < 3 ? q : (q == 3 ? 1 : 2);
+        const double l = (-fbank(d, b, q)[c]) + uh[a][c] * uh[bb][c];
+        const double dout = fbank(d, b, 6 + q)[c];
+        const double fac = a == bb ? 0.5 : 0.25;
+        const double hs = S[3 * a + bb] / fac;
+        double m = ((4.0 * magh) * fac) * hs;
         m = fw2 * (m - dout);
         if (q == 0) {
             lm = l * m;
@@ -1215,32 +1272,31 @@ __global__ void k3_germano6(D3 d)
             lm = lm + l * m;
             mm = mm + m * m;
         } else {
-            lm = lm + (T(2) * l) * m;
-            mm = mm + (T(2) * m) * m;
+            lm = lm + (2.0 * l) * m;
+            mm = mm + (2.0 * m) * m;
         }
     }
-    d.LM[c] = (double)lm;
-    d.MM[c] = (double)mm;
+    d.LM[c] = lm;
+    d.MM[c] = mm;
 }
 
-// Temperature terms P_q, R_q of the three heat-flux components
-// (stress_tensor_dy.f90:590-680) accumulated into LM and MM.
-template <class T>
-__global__ void k3_germano_t3(D3 d)
+// Temperature terms P_q, R_q of the three heat-flux components from the filtered
+// products in bank b, accumulated into LM and MM.
+__global__ void k3_germano_t(D3 d, int b)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
-    const double *uf[3] = {d.U, d.V, d.W}, *uh[3] = {d.UH, d.VH, d.WH};
+    const double *uh[3] = {d.UH, d.VH, d.WH};
     const double *M1[3] = {d.XIX, d.XIY, d.XIZ}, *M2[3] = {d.ETX, d.ETY, d.ETZ}, *M3[3] = {d.ZTX, d.ZTY, d.ZTZ};
-    const T fw2 = T(d.FW[c]) * T(d.FW[c]), magh = T(d.MAGH[c]);
-    T lm = T(0), mm = T(0);
+    const double fw2 = d.FW[c] * d.FW[c], magh = d.MAGH[c];
+    double lm = 0.0, mm = 0.0;
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        const T l = (-filt2<T>(d, uf[q], d.T, i, j, k)) + T(uh[q][c]) * T(d.TH[c]);
-        const T dout = filt2<T>(d, d.MAG, d.DTD[q], i, j, k);
-        const T g = (dxi<T>(d, M1[q], d.TH, i, j, k) + deta<T>(d, M2[q], d.TH, i, j, k)) +
-                    dzeta<T>(d, M3[q], d.TH, i, j, k);
-        T m = ((T(4) * magh) * T(0.5)) * g;
+        const double l = (-fbank(d, b, q)[c]) + uh[q][c] * d.TH[c];
+        const double dout = fbank(d, b, 3 + q)[c];
+        const double g = (dxi<double>(d, M1[q], d.TH, i, j, k) + deta<double>(d, M2[q], d.TH, i, j, k)) +
+                         dzeta<double>(d, M3[q], d.TH, i, j, k);
+        double m = ((4.0 * magh) * 0.5) * g;
         m = fw2 * (m - dout);
         if (q == 0) {
             lm = l * m;
@@ -1250,8 +1306,8 @@ __global__ void k3_germano_t3(D3 d)
             mm = mm + m * m;
         }
     }
-    d.LM[c] = (double)lm;
-    d.MM[c] = (double)mm;
+    d.LM[c] = lm;
+    d.MM[c] = mm;
 }
 
 // Volume-averaged coefficient over the points whose local coefficient is >= 0
@@ -1578,6 +1634,7 @@ void carve(Bump &b, fvm3_ctx *c)
     }
     float **f32[] = {&d.RF, &d.DF, &d.ANf, &d.ASf, &d.ATf, &d.ABf};
     for (auto p : f32) *p = reinterpret_cast<float *>(b.take((n + 1) / 2));
+    d.FB = b.take(24 * n);
     d.nblk = 8 * 152;   // residual and reduction kernels: 8 blocks of 256 threads per SM
     d.partial = b.take(4 * size_t(d.nblk));
     d.pctl = reinterpret_cast<PCtl *>(b.take(8));
@@ -1703,7 +1760,8 @@ int predictor(fvm3_ctx *c, int kind, double *phi, const double *phin, const doub
     D3 &d = c->d;
     const int base = kind == 2 ? 3 : 0;
     for (int split = 0; split < 3; split++) {
-        k3_af_rhs<<<g_int(c), B_INT, 0, c->stream>>>(d, d.cf[base + split], split, kind, phi, phin, ina, inb, inc, ind, ff);
+        auto rhs = c->p.precision == FVM_MIXED ? k3_af_rhs<float> : k3_af_rhs<double>;
+        rhs<<<g_int(c), B_INT, 0, c->stream>>>(d, d.cf[base + split], split, kind, phi, phin, ina, inb, inc, ind, ff);
         k3_ghost<<<dim3((c->NJ + 1 + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, phi, ff, kind);
         F3RC(halo(c, {phi}));
         F3RC(line(c, base + split, d.SU, phi, 0));
@@ -1785,6 +1843,22 @@ int poisson(fvm3_ctx *c)
     return FVM_OK;
 }
 
+// The separable test filter of the inputs of `mode` (SEP_HATS: into UH, VH, WH,
+// TH; otherwise into bank 1).
+int sep_filter(fvm3_ctx *c, int mode)
+{
+    D3 &d = c->d;
+    const int nq = mode == SEP_HATS ? 4 : (mode == SEP_VEL ? 12 : 6);
+    Out4 none{}, hats{};
+    if (mode == SEP_HATS) hats = Out4{{d.UH, d.VH, d.WH, d.TH}};
+    k3_prod<<<g_lin(c), 256, 0, c->stream>>>(d, mode);
+    k3_sep<<<dim3((c->NI - 1 + 31) / 32, (c->NJ + 1 + 3) / 4, c->NK + 1), B_INT, 0, c->stream>>>(d, 0, 1, nq, 0, none);
+    k3_sep<<<dim3((c->NI - 1 + 31) / 32, (c->NJ - 1 + 3) / 4, c->NK + 1), B_INT, 0, c->stream>>>(d, 1, 0, nq, 1, none);
+    k3_sep<<<g_int(c), B_INT, 0, c->stream>>>(d, 0, 1, nq, 2, mode == SEP_HATS ? hats : none);
+    F3CHECK(c);
+    return FVM_OK;
+}
+
 int sgs(fvm3_ctx *c)
 {
     D3 &d = c->d;
@@ -1793,23 +1867,20 @@ int sgs(fvm3_ctx *c)
     F3RC(halo(c, {d.L[0], d.L[1], d.L[2], d.L[3], d.L[4], d.L[5], d.L[6], d.L[7], d.L[8], d.DTD[0], d.DTD[1],
                   d.DTD[2]}));
     k3_mag<<<g_lin(c), 256, 0, st>>>(d);
-    const bool f32 = c->p.precision == FVM_MIXED;   // the model's stencils in FP32
-    auto filter = f32 ? k3_filter<float> : k3_filter<double>;
-    filter<<<g_int(c), B_INT, 0, st>>>(d, d.U, d.UH);
-    filter<<<g_int(c), B_INT, 0, st>>>(d, d.V, d.VH);
-    filter<<<g_int(c), B_INT, 0, st>>>(d, d.W, d.WH);
-    filter<<<g_int(c), B_INT, 0, st>>>(d, d.T, d.TH);
+    F3RC(sep_filter(c, SEP_HATS));
     F3RC(bcu(c, d.UH, d.FFU, 0));
     F3RC(bcu(c, d.VH, d.FFV, 1));
     F3RC(bcu(c, d.WH, d.FFW, 1));
     F3RC(bcu(c, d.TH, d.FFT, 2));
-    (f32 ? k3_germano6<float> : k3_germano6<double>)<<<g_int(c), B_INT, 0, st>>>(d);
+    F3RC(sep_filter(c, SEP_VEL));
+    k3_germano<<<g_int(c), B_INT, 0, st>>>(d, 1);
     if (d.les_zavg) k3_czavg<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1), 128, 0, st>>>(d);
     else k3_cvol<<<d.nblk, 256, 0, st>>>(d, 0);
     k3_eddy<<<g_lin(c), 256, 0, st>>>(d, 0, d.EV);
     k3_sgs<<<g_int(c), B_INT, 0, st>>>(d);
     if (d.thermal) {
-        (f32 ? k3_germano_t3<float> : k3_germano_t3<double>)<<<g_int(c), B_INT, 0, st>>>(d);
+        F3RC(sep_filter(c, SEP_HEAT));
+        k3_germano_t<<<g_int(c), B_INT, 0, st>>>(d, 1);
         if (d.les_zavg) k3_czavg<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1), 128, 0, st>>>(d);
         else k3_cvol<<<d.nblk, 256, 0, st>>>(d, 1);
         k3_eddy<<<g_lin(c), 256, 0, st>>>(d, 1, d.EC);
@@ -1837,53 +1908,127 @@ int read_coeffs(fvm3_ctx *c, fvm3_coeffs *out)
     return FVM_OK;
 }
 
-int step(fvm3_ctx *c)
+// The routines of the time loop (main.f90:33-147), one host function per call point.
+int begin_step(fvm3_ctx *c)   // main.f90:37-44, the far-field values of BCU/BCT from the step-n fields
 {
     D3 &d = c->d;
-    cudaStream_t st = c->stream;
     c->niter_time += 1;
     c->rtime = c->rtime + d.dt;
-    k3_begin<<<g_lin(c), 256, 0, st>>>(d);
-    k3_farfield<<<dim3((c->NJ + 127) / 128, c->NK - 1), 128, 0, st>>>(d);
-    k3_contra<<<g_lin(c), 256, 0, st>>>(d);
-    F3RC(halo(c, {d.U1, d.U2, d.U3}));
-    k3_fluxes<<<g_int(c), B_INT, 0, st>>>(d, 0);
-    k3_explicit<<<g_int(c), B_INT, 0, st>>>(d, d.thermal);
-    F3CHECK(c);
-    if (c->p.use_les) F3RC(sgs(c));
-    k3_dif<<<g_int(c), B_INT, 0, st>>>(d, d.thermal);
-    k3_psource<<<g_int(c), B_INT, 0, st>>>(d);
-    F3CHECK(c);
-    F3RC(predictor(c, 0, d.U, d.U_N, d.NLX, d.NLX_NM1, d.DIFX, d.S_U, d.FFU));
-    F3RC(predictor(c, 1, d.V, d.V_N, d.NLY, d.NLY_NM1, d.DIFY, d.S_V, d.FFV));
-    F3RC(predictor(c, 1, d.W, d.W_N, d.NLZ, d.NLZ_NM1, d.DIFZ, d.S_W, d.FFW));
-    k3_grad<<<g_int(c), B_INT, 0, st>>>(d, -1.0);
-    F3RC(bcu(c, d.U, d.FFU, 0));
-    F3RC(bcu(c, d.V, d.FFV, 1));
-    F3RC(bcu(c, d.W, d.FFW, 1));
-    k3_contra<<<g_lin(c), 256, 0, st>>>(d);
-    F3RC(halo(c, {d.U1, d.U2, d.U3}));
-    k3_fluxes<<<g_int(c), B_INT, 0, st>>>(d, 1);
-    F3CHECK(c);
-    F3RC(poisson(c));
-    k3_bcp<<<dim3((c->NJ + 127) / 128, c->NK + 1), 128, 0, st>>>(d, 0);
-    F3RC(halo(c, {d.P}));
-    k3_psource<<<g_int(c), B_INT, 0, st>>>(d);
-    k3_grad<<<g_int(c), B_INT, 0, st>>>(d, +1.0);
-    k3_pref<<<1, 32, 0, st>>>(d);
-    k3_pshift<<<g_lin(c), 256, 0, st>>>(d);
-    F3RC(bcu(c, d.U, d.FFU, 0));
-    F3RC(bcu(c, d.V, d.FFV, 1));
-    F3RC(bcu(c, d.W, d.FFW, 1));
-    if (d.thermal) {
-        F3RC(predictor(c, 2, d.T, d.T_N, d.ADV, d.ADV_NM1, d.DIFT, nullptr, d.FFT));
-        F3RC(bcu(c, d.T, d.FFT, 2));
-    }
-    k3_cfl<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1, c->NK - 1), 128, 0, st>>>(d);
-    k3_wall<<<dim3((c->NJ + 127) / 128, c->NK - 1, 2), 128, 0, st>>>(d);
-    k3_calc_final<<<1, 1024, 0, st>>>(d, c->rtime, c->sum_area);
+    k3_begin<<<g_lin(c), 256, 0, c->stream>>>(d);
+    k3_farfield<<<dim3((c->NJ + 127) / 128, c->NK - 1), 128, 0, c->stream>>>(d);
     F3CHECK(c);
     return FVM_OK;
+}
+
+int contra_vel(fvm3_ctx *c, int with_div)   // CONTRA_VEL; with_div: the Poisson source too
+{
+    D3 &d = c->d;
+    k3_contra<<<g_lin(c), 256, 0, c->stream>>>(d);
+    F3RC(halo(c, {d.U1, d.U2, d.U3}));
+    k3_fluxes<<<g_int(c), B_INT, 0, c->stream>>>(d, with_div);
+    F3CHECK(c);
+    return FVM_OK;
+}
+
+int nl_all(fvm3_ctx *c)   // main.f90:50-57
+{
+    k3_explicit<<<g_int(c), B_INT, 0, c->stream>>>(c->d, c->d.thermal);
+    F3CHECK(c);
+    return FVM_OK;
+}
+
+int dif_all(fvm3_ctx *c)   // main.f90:72-75
+{
+    auto dif = c->p.precision == FVM_MIXED ? k3_dif<float> : k3_dif<double>;
+    dif<<<g_int(c), B_INT, 0, c->stream>>>(c->d, c->d.thermal);
+    F3CHECK(c);
+    return FVM_OK;
+}
+
+int p_source(fvm3_ctx *c)   // P_SOURCE(P)
+{
+    k3_psource<<<g_int(c), B_INT, 0, c->stream>>>(c->d);
+    F3CHECK(c);
+    return FVM_OK;
+}
+
+int iter_u(fvm3_ctx *c, int comp)   // ITER_U of U (0), V (1) or W (2), main.f90:81-88
+{
+    D3 &d = c->d;
+    if (comp == 0) return predictor(c, 0, d.U, d.U_N, d.NLX, d.NLX_NM1, d.DIFX, d.S_U, d.FFU);
+    if (comp == 1) return predictor(c, 1, d.V, d.V_N, d.NLY, d.NLY_NM1, d.DIFY, d.S_V, d.FFV);
+    return predictor(c, 1, d.W, d.W_N, d.NLZ, d.NLZ_NM1, d.DIFZ, d.S_W, d.FFW);
+}
+
+int bcu_all(fvm3_ctx *c)   // BCU of U, V, W
+{
+    D3 &d = c->d;
+    F3RC(bcu(c, d.U, d.FFU, 0));
+    F3RC(bcu(c, d.V, d.FFV, 1));
+    F3RC(bcu(c, d.W, d.FFW, 1));
+    return FVM_OK;
+}
+
+int remove_grad(fvm3_ctx *c)   // main.f90:90-97: u -= dt S/J, BCU
+{
+    k3_grad<<<g_int(c), B_INT, 0, c->stream>>>(c->d, -1.0);
+    F3CHECK(c);
+    return bcu_all(c);
+}
+
+int iter_p(fvm3_ctx *c)   // main.f90:99-104: CONTRA_VEL, ITER_P, BCP
+{
+    D3 &d = c->d;
+    F3RC(contra_vel(c, 1));
+    F3RC(poisson(c));
+    k3_bcp<<<dim3((c->NJ + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, 0);
+    F3RC(halo(c, {d.P}));
+    return FVM_OK;
+}
+
+int correct(fvm3_ctx *c)   // main.f90:106-140: P_SOURCE, u += dt S/J, reference pressure, BCU
+{
+    D3 &d = c->d;
+    k3_psource<<<g_int(c), B_INT, 0, c->stream>>>(d);
+    k3_grad<<<g_int(c), B_INT, 0, c->stream>>>(d, +1.0);
+    k3_pref<<<1, 32, 0, c->stream>>>(d);
+    k3_pshift<<<g_lin(c), 256, 0, c->stream>>>(d);
+    F3CHECK(c);
+    return bcu_all(c);
+}
+
+int iter_t(fvm3_ctx *c)   // main.f90:143-145: ITER_T, BCT
+{
+    D3 &d = c->d;
+    if (!d.thermal) return FVM_OK;
+    F3RC(predictor(c, 2, d.T, d.T_N, d.ADV, d.ADV_NM1, d.DIFT, nullptr, d.FFT));
+    return bcu(c, d.T, d.FFT, 2);
+}
+
+int calccoef(fvm3_ctx *c)   // CALCCOEF kernels; the record is read by read_coeffs
+{
+    D3 &d = c->d;
+    k3_cfl<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1, c->NK - 1), 128, 0, c->stream>>>(d);
+    k3_wall<<<dim3((c->NJ + 127) / 128, c->NK - 1, 2), 128, 0, c->stream>>>(d);
+    k3_calc_final<<<1, 1024, 0, c->stream>>>(d, c->rtime, c->sum_area);
+    F3CHECK(c);
+    return FVM_OK;
+}
+
+int step(fvm3_ctx *c)
+{
+    F3RC(begin_step(c));
+    F3RC(contra_vel(c, 0));
+    F3RC(nl_all(c));
+    if (c->p.use_les) F3RC(sgs(c));
+    F3RC(dif_all(c));
+    F3RC(p_source(c));
+    for (int comp = 0; comp < 3; comp++) F3RC(iter_u(c, comp));
+    F3RC(remove_grad(c));
+    F3RC(iter_p(c));
+    F3RC(correct(c));
+    F3RC(iter_t(c));
+    return calccoef(c);
 }
 
 double *array_by_name(fvm3_ctx *c, const char *name)
@@ -2096,6 +2241,71 @@ int fvm3_sgs(fvm3_ctx *c, fvm3_coeffs *out)
         out->cs2 = s[0];
         out->ct2 = s[1];
     }
+    return FVM_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Per-routine call points (fvm3_step runs them in this order)
+// ---------------------------------------------------------------------------------
+#define F3READY(c)                                                        \
+    do {                                                                  \
+        if (!(c)) return FVM_ERR_ARG;                                     \
+        if (!(c)->init_done) return f3::bad3((c), "fvm3_init has not been called"); \
+    } while (0)
+
+int fvm3_begin_step(fvm3_ctx *c) { F3READY(c); return f3::begin_step(c); }
+int fvm3_contra_vel(fvm3_ctx *c) { F3READY(c); return f3::contra_vel(c, 0); }
+int fvm3_nl(fvm3_ctx *c) { F3READY(c); return f3::nl_all(c); }
+int fvm3_stress_tensor(fvm3_ctx *c)
+{
+    F3READY(c);
+    return c->p.use_les ? f3::sgs(c) : FVM_OK;
+}
+int fvm3_dif(fvm3_ctx *c) { F3READY(c); return f3::dif_all(c); }
+int fvm3_p_source(fvm3_ctx *c) { F3READY(c); return f3::p_source(c); }
+int fvm3_iter_u(fvm3_ctx *c, int component)
+{
+    F3READY(c);
+    if (component < 0 || component > 2) return f3::bad3(c, "component must be 0 (U), 1 (V) or 2 (W)");
+    return f3::iter_u(c, component);
+}
+int fvm3_remove_grad(fvm3_ctx *c) { F3READY(c); return f3::remove_grad(c); }
+int fvm3_iter_p(fvm3_ctx *c, double *resid, int *sweeps)
+{
+    F3READY(c);
+    F3RC(f3::iter_p(c));
+    F3CUDA(c, cudaMemcpyAsync(c->h_pctl, c->d.pctl, sizeof(fvm::PCtl), cudaMemcpyDeviceToHost, c->stream));
+    F3CUDA(c, cudaStreamSynchronize(c->stream));
+    if (resid) *resid = c->h_pctl->resip;
+    if (sweeps) *sweeps = c->h_pctl->niter;
+    if (!std::isfinite(c->h_pctl->resip)) {
+        c->err = "non-finite Poisson residual";
+        return FVM_ERR_NAN;
+    }
+    return c->h_pctl->capped ? FVM_ERR_NOCONV : FVM_OK;
+}
+int fvm3_correct(fvm3_ctx *c) { F3READY(c); return f3::correct(c); }
+int fvm3_iter_t(fvm3_ctx *c) { F3READY(c); return f3::iter_t(c); }
+int fvm3_calccoef(fvm3_ctx *c, fvm3_coeffs *out)
+{
+    F3READY(c);
+    F3RC(f3::calccoef(c));
+    return f3::read_coeffs(c, out);
+}
+
+int fvm3_test_filter(fvm3_ctx *c, const double *in, double *out)
+{
+    if (!c || !in || !out) return f3::bad3(c, "null argument");
+    if (!c->grid_set) return f3::bad3(c, "fvm3_set_grid has not been called");
+    f3::D3 &d = c->d;
+    const size_t bytes = sizeof(double) * c->n;
+    // LM and MM are scratch of the SGS model between its own kernels
+    F3CUDA(c, cudaMemcpyAsync(d.LM, in, bytes, cudaMemcpyHostToDevice, c->stream));
+    F3CUDA(c, cudaMemcpyAsync(d.MM, out, bytes, cudaMemcpyHostToDevice, c->stream));
+    f3::k3_filter<double><<<f3::g_int(c), f3::B_INT, 0, c->stream>>>(d, d.LM, d.MM);
+    F3CHECK(c);
+    F3CUDA(c, cudaMemcpyAsync(out, d.MM, bytes, cudaMemcpyDeviceToHost, c->stream));
+    F3CUDA(c, cudaStreamSynchronize(c->stream));
     return FVM_OK;
 }
 

@@ -32,7 +32,11 @@ typedef struct fvm3_params {
     int res_every;         /* Poisson residual every k-th sweep */
     double ref_a;          /* reference area of the force coefficients (REF_A) */
     int precision;         /* FVM_FP64, or FVM_MIXED: FP32 red-black Poisson sweeps on the
-                              correction inside FP64 residual refinement */
+                              correction inside FP64 residual refinement; DIF and the
+                              predictor's cross terms summed in FP32 from FP64 differences;
+                              metrics, residuals, the SGS model (its Leonard term cancels
+                              to ~1e-6 of its operands), the predictor's line solves and
+                              the state stay FP64 */
     int refine_sweeps;     /* MIXED: FP32 sweeps per FP64 residual */
     int device;
 } fvm3_params;
@@ -58,6 +62,40 @@ int fvm3_set_grid(struct fvm3_ctx *ctx, const double *xg, const double *yg, cons
 int fvm3_init(struct fvm3_ctx *ctx, const double *du, const double *dv, const double *dw);
 /* nsteps time steps (main.f90:33-147); out (may be NULL): the last step's record. */
 int fvm3_step(struct fvm3_ctx *ctx, int nsteps, fvm3_coeffs *out);
+/* Per-routine call points of the time loop, in the order fvm3_step runs them
+ * (main.f90:33-147), for a driver that keeps some routines of its own:
+ *   fvm3_begin_step     NITER_TIME, RTIME, U_N..T_N = U..T (main.f90:37-44), and the
+ *                       far-field values BCU/BCT use during the step (bcu.f90:30-40)
+ *   fvm3_contra_vel     CONTRA_VEL (contra_vel.f90:13-56)
+ *   fvm3_nl             NLX..ADV kept as *_NM1, NL of U_N, V_N, W_N, T_N (main.f90:50-57)
+ *   fvm3_stress_tensor  STRESS_TENSOR_DY and the SGS terms added to NLX..ADV
+ *                       (main.f90:59-69); nothing when use_les = 0
+ *   fvm3_dif            DIF of U_N, V_N, W_N, T_N (main.f90:72-75)
+ *   fvm3_p_source       P_SOURCE(P) (p_source.f90:14-42)
+ *   fvm3_iter_u         ITER_U of U (component 0), V (1) or W (2) (iter_u.f90:23-255)
+ *   fvm3_remove_grad    u -= dt S/J, then BCU of U, V, W (main.f90:90-97)
+ *   fvm3_iter_p         CONTRA_VEL, ITER_P, BCP (main.f90:99-104); resid and sweeps
+ *                       may be NULL; FVM_ERR_NOCONV when the sweep cap ended it
+ *   fvm3_correct        P_SOURCE, u += dt S/J, the far-field reference pressure,
+ *                       BCU (main.f90:106-140)
+ *   fvm3_iter_t         ITER_T, BCT (main.f90:143-145); nothing when thermal = 0
+ *   fvm3_calccoef       CALCCOEF; out may be NULL */
+int fvm3_begin_step(struct fvm3_ctx *ctx);
+int fvm3_contra_vel(struct fvm3_ctx *ctx);
+int fvm3_nl(struct fvm3_ctx *ctx);
+int fvm3_stress_tensor(struct fvm3_ctx *ctx);
+int fvm3_dif(struct fvm3_ctx *ctx);
+int fvm3_p_source(struct fvm3_ctx *ctx);
+int fvm3_iter_u(struct fvm3_ctx *ctx, int component);
+int fvm3_remove_grad(struct fvm3_ctx *ctx);
+int fvm3_iter_p(struct fvm3_ctx *ctx, double *resid, int *sweeps);
+int fvm3_correct(struct fvm3_ctx *ctx);
+int fvm3_iter_t(struct fvm3_ctx *ctx);
+int fvm3_calccoef(struct fvm3_ctx *ctx, fvm3_coeffs *out);
+/* TEST_FILTER(IN, OUT) (test_filter.f90:13-21): the [1,2,1]^3/64 box filter of the
+ * host array in into the interior of the host array out (its other entries are
+ * left as passed).  Needs the grid only. */
+int fvm3_test_filter(struct fvm3_ctx *ctx, const double *in, double *out);
 /* Named arrays ("U","V","W","P","T","NLX","NLY","NLZ","ADV","DJAC","SGS_X",...). */
 int fvm3_get_array(struct fvm3_ctx *ctx, const char *name, double *out);
 int fvm3_set_array(struct fvm3_ctx *ctx, const char *name, const double *in);

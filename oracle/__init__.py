@@ -229,6 +229,7 @@ class Oracle3D:
             L.o3_array.restype = P
             L.o3_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
             L.o3_sgs.argtypes = [ctypes.c_void_p]
+            L.o3_test_filter.argtypes = [ctypes.c_void_p, P, P]
             L._o3_ready = True
         self.ni, self.nj, self.nk = ni, nj, nk
         if ref_a is None:
@@ -265,6 +266,14 @@ class Oracle3D:
 
     def sgs(self):
         lib().o3_sgs(self._h)
+
+    def test_filter(self, a, out=None):
+        """TEST_FILTER(IN, OUT) of a into the interior of out (test_filter.f90)."""
+        shape = (self.nk + 1, self.nj + 1, self.ni + 1)
+        src = np.ascontiguousarray(a, dtype=np.float64).reshape(shape)
+        dst = np.zeros(shape) if out is None else np.array(out, dtype=np.float64).reshape(shape)
+        lib().o3_test_filter(self._h, _dptr(src), _dptr(dst))
+        return dst
 
     def array(self, name) -> np.ndarray:
         p = lib().o3_array(self._h, name.encode())

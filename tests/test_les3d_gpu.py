@@ -91,3 +91,63 @@ def test_mixed_sweep_cap_is_reported():
     g, o, ctx = _case(precision=capi.MIXED, refine_sweeps=8, resimax=1e-30, nswpp=40)
     c = ctx.step(1)
     assert c["sweeps"] == 40 and c["resid"] > 1e-30
+
+
+def test_per_routine_call_points_equal_the_step():
+    """The call points of fvm3d.h in the reference's order give the step bit for bit."""
+    g, o, a = _case(resimax=1e-8, nswpp=4000)
+    _, _, b = _case(resimax=1e-8, nswpp=4000)
+    for s in range(2):
+        ca = a.step(1)
+        b.call("begin_step")
+        b.call("contra_vel")
+        b.call("nl")
+        b.call("stress_tensor")
+        b.call("dif")
+        b.call("p_source")
+        for comp in range(3):
+            b.iter_u(comp)
+        b.call("remove_grad")
+        resid, sweeps = b.iter_p()
+        b.call("correct")
+        b.call("iter_t")
+        cb = b.calccoef()
+        assert sweeps == ca["sweeps"] and resid == ca["resid"], s
+        assert cb["cd"] == ca["cd"] and cb["nu"] == ca["nu"], s
+    for nm in ("U", "V", "W", "P", "T", "NLX", "ADV"):
+        assert np.array_equal(a.get(nm), b.get(nm)), nm
+
+
+def test_test_filter_matches_the_restatement():
+    g, o, ctx = _case()
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal(ctx.shape)
+    keep = rng.standard_normal(ctx.shape)
+    got = ctx.test_filter(x, keep)
+    ref = o.test_filter(x, keep)
+    assert np.allclose(got, ref, rtol=1e-14, atol=1e-15)
+    # entries outside the interior are left as passed
+    assert np.array_equal(got[0], keep[0]) and np.array_equal(got[:, :, -1], keep[:, :, -1])
+
+
+def test_mixed_tracks_fp64_on_a_wall_resolved_grid():
+    """On a grid with the first radial spacing of the LES configuration (0.001 D)
+    the mixed path stays close to the FP64 path over several steps.  Both stop the
+    Poisson iteration at the same sweep cap, so they differ by the unconverged
+    remainders (~1e-5), not by the precision of the stencils."""
+    g = o_grid_3d(64, 48, 16, lz=np.pi, dr1=0.001)
+    du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, 0.05, 0)
+    out = {}
+    for prec in (capi.FP64, capi.MIXED):
+        p = capi3d.default_params(ni=g.ni, nj=g.nj, nk=g.nk, re=3900.0, dt=0.002, resimax=1e-12, nswpp=200,
+                                  use_les=1, les_zavg=1, thermal=1, res_every=4, ref_a=np.pi, precision=prec,
+                                  refine_sweeps=20)
+        ctx = capi3d.Context3(p)
+        ctx.set_grid(g)
+        ctx.init(du, dv, dw)
+        c = ctx.step(6)
+        out[prec] = ({nm: ctx.get(nm) for nm in ("U", "V", "W", "P", "T")}, c["cd"])
+        ctx.close()
+    for nm in ("U", "V", "W", "T"):
+        assert rel_l2(out[capi.MIXED][0][nm], out[capi.FP64][0][nm]) <= 1e-3, nm
+    assert abs(out[capi.MIXED][1] - out[capi.FP64][1]) <= 1e-3 * abs(out[capi.FP64][1])
