@@ -390,6 +390,8 @@ def run_adjoint_bench(args):
 LES3D = dict(name="les3d-re3900-256x192x48", n_theta=256, n_r=192, n_z=48, re=3900.0, pr=0.71, dt=0.002,
              dr1=0.001, amp=0.05, seed=0, resimax=1e-10, nswpp=200, res_every=4, refine_sweeps=20, zavg=1,
              thermal=1)
+# the same case on a smaller grid, for ncu captures that replay kernels many times
+LES3D_PROFILE = dict(LES3D, name="les3d-re3900-192x160x32", n_theta=192, n_r=160, n_z=32)
 FIELDS3D = ("U", "V", "W", "P", "T", "NLX", "NLY", "NLZ", "ADV")
 
 
@@ -466,7 +468,7 @@ def run_les3d_bench(args):
     rank, world = dist.init("nccl")
     local = dist.rank_world()[2]
     torch.cuda.set_device(local)
-    w = dict(LES3D)
+    w = dict(LES3D_PROFILE if args.les3d_grid == "profile" else LES3D)
     g, du, dv, dw = les3d_inputs(w)
     n_int = (g.ni - 1) * (g.nj - 1) * (g.nk - 1)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -751,6 +753,8 @@ def main():
                          "adjoint: window-drag gradient on the 128x96 grid; "
                          "les3d: 3-D LES on the 256x192x48 grid, FP64 and mixed")
     ap.add_argument("--spinup", type=int, default=200, help="adjoint workload: steps before the window")
+    ap.add_argument("--les3d-grid", choices=["full", "profile"], default="full",
+                    help="les3d: the 256x192x48 grid, or 192x160x32 for profiler captures")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
