@@ -641,6 +641,105 @@ __global__ void __launch_bounds__(256) k_adj_pres(Dev d, Adj a, int per, double 
     }
 }
 
+// MIXED: the transposed Poisson equation by FP64 defect correction around FP32 zebra
+// sweeps, as the forward solve.  Each outer iteration forms in FP64 the residual
+// r = g - XD(mu) - A^T mu with the cross term of the current mu, its scaled L1 norm
+// (the convergence test) and r in FP32; refine_sweeps FP32 zebra sweeps solve
+// A^T dmu = r from dmu = 0; mu += dmu in FP64.
+__global__ void __launch_bounds__(256) k_adj_mres(Dev d, Adj a, double tol, int nmax)
+{
+    __shared__ double sh[64];
+    __shared__ bool last;
+    if (a.pctl->done) return;
+    Dev da = d;
+    da.pctl = a.pctl;
+    da.partial = a.partial;
+    const int it = a.pctl->niter;
+    const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
+    const Coef &cf = a.cPT;
+    double ra = 0.0, pa = 0.0;
+#pragma unroll
+    for (int q = 0; q < RES_CELLS; q++) {
+        int e = (blockIdx.x * RES_CELLS + q) * 256 + threadIdx.x;
+        if (e < total) {
+            int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
+            const double *mu = a.mu;
+            double am = cf.AP[c] * mu[c] - cf.AE[c] * mu[IDX(i + 1, j)] - cf.AW[c] * mu[IDX(i - 1, j)] -
+                        cf.AN[c] * mu[IDX(i, jwrap(d, j + 1))] - cf.AS[c] * mu[IDX(i, jwrap(d, j - 1))];
+            double r = (a.g[c] - xd_at(d, mu, i, j)) - am;
+            ra += fabs(r);
+            pa += fabs(cf.AP[c] * mu[c]);
+            d.RF[c] = (float)r;
+            d.DF[c] = 0.0f;
+        }
+    }
+    if (!grid_sum2(da, ra, pa, sh, last)) return;
+    if (threadIdx.x == 0) {
+        const double resip = pa > 0.0 ? ra / pa : 0.0;
+        a.pctl->resip = resip;
+        if (it > 0 && !(resip > tol && it < nmax)) {
+            a.pctl->done = 1;
+            a.pctl->capped = resip > tol ? 1 : 0;
+        } else {
+            a.pctl->niter = it + d.refine_sweeps;
+        }
+    }
+}
+
+template <int M, int NW>
+__global__ void __launch_bounds__(128) k_adj_pois32(Dev d, Adj a, int colour)
+{
+    constexpr int TG = WARP * NW, G = 4 / NW;
+    __shared__ float sm[G][TG * M + M * NW + 1];
+    __shared__ float xch[G][2 * NW];
+    if (a.pctl->done) return;
+    int gl, t, gib;
+    group_of<NW>(gl, t, gib);
+    const bool active = gl < (d.NJ - 1) / 2;
+    const int j = active ? 2 * gl + 1 + colour : 1;
+    const int jn = jwrap(d, j + 1), js = jwrap(d, j - 1);
+    const LineSys &s = a.sPT;
+    const Coef &cf = a.cPT;
+    const int n = s.n;
+    float v[M];
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        int e = k * TG + t;
+        v[k] = 0.0f;
+        if (active && e < n) {
+            const int c = IDX(e + 1, j);
+            v[k] = (cf.ANf[c] * d.DF[IDX(e + 1, jn)] + cf.ASf[c] * d.DF[IDX(e + 1, js)]) + d.RF[c];
+        }
+    }
+    to_chunks<float, M, NW>(v, sm[gib], t);
+    const size_t base = size_t(j - 1) * TG * M;
+    group_apply<float, M, NW>(v, s.invDf + base, s.faf + base, s.fbf + base, t, xch[gib]);
+    to_interleaved<float, M, NW>(v, sm[gib], t);
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        int e = k * TG + t;
+        if (active && e < n) d.DF[IDX(e + 1, j)] = v[k];
+    }
+}
+
+__global__ void k_adj_apply(Dev d, Adj a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+    if (i > d.NI - 1 || j > d.NJ - 1) return;
+    if (a.pctl->done) return;
+    const int c = IDX(i, j);
+    a.mu[c] = a.mu[c] + (double)d.DF[c];
+}
+
+__global__ void k_adj_coef_f32(Dev d, Coef cf)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+    if (i > d.NI - 1 || j > d.NJ - 1) return;
+    const int c = IDX(i, j);
+    cf.ANf[c] = (float)cf.AN[c];
+    cf.ASf[c] = (float)cf.AS[c];
+}
+
 __global__ void k_adj_pctl_reset(Adj a)
 {
     a.pctl->niter = 0;
@@ -713,6 +812,8 @@ void carve_coef_t(char *&p, Coef &cf, size_t n)
     cf.AW = take(n);
     cf.AN = take(n);
     cf.AS = take(n);
+    cf.ANf = reinterpret_cast<float *>(take((n + 1) / 2));
+    cf.ASf = reinterpret_cast<float *>(take((n + 1) / 2));
 }
 
 void carve_sys_t(char *&p, LineSys &s, const LineSys &like)
@@ -728,9 +829,9 @@ void carve_sys_t(char *&p, LineSys &s, const LineSys &like)
     s.invD = take(cnt);
     s.fa = take(cnt);
     s.fb = take(cnt);
-    s.invDf = nullptr;
-    s.faf = nullptr;
-    s.fbf = nullptr;
+    s.invDf = reinterpret_cast<float *>(take((cnt + 1) / 2));   // FP32 factors (mixed Poisson adjoint)
+    s.faf = reinterpret_cast<float *>(take((cnt + 1) / 2));
+    s.fbf = reinterpret_cast<float *>(take((cnt + 1) / 2));
     s.zf = nullptr;
     s.cvf = nullptr;
     s.sinvf = nullptr;
@@ -783,6 +884,12 @@ __global__ void k_adj_factor(Dev d, Coef cf, LineSys s, int circ)
         s.fa[k] = 0.0;
         s.fb[k] = 0.0;
     }
+    for (int e = 0; e < TG * M; e++) {
+        size_t k = slot(e);
+        s.invDf[k] = (float)s.invD[k];
+        s.faf[k] = (float)s.fa[k];
+        s.fbf[k] = (float)s.fb[k];
+    }
     if (circ) {
         double y = 0.0;
         for (int e = 0; e < n; e++) {
@@ -816,9 +923,11 @@ int adj_setup(fvm_ctx *c)
     const size_t nj1 = c->NJ + 1;
     auto sys_bytes = [](const LineSys &s) {
         size_t cnt = size_t(s.lines) * WARP * s.NW * s.M;
-        return (4 * cnt + 2 * s.lines) * sizeof(double) + 8 * 256;
+        // invD, fa, fb, z (FP64), their FP32 copies, cv, sinv, alignment
+        return (6 * cnt + 2 * s.lines) * sizeof(double) + 16 * 256;
     };
-    size_t bytes = (30 * n + 10 * nj1 + 16) * sizeof(double) + 3 * 5 * (n * sizeof(double) + 256) +
+    // per transposed set: AP, AE, AW, AN, AS (FP64) and ANf, ASf (FP32)
+    size_t bytes = (30 * n + 10 * nj1 + 16) * sizeof(double) + 3 * (6 * n * sizeof(double) + 8 * 256) +
                    sys_bytes(d.sP) + sys_bytes(d.sUX) + sys_bytes(d.sUY) + 64 * 256 + sizeof(PCtl) +
                    2 * size_t(c->nblk_res) * sizeof(double);
     cudaError_t e = cudaMalloc(&A->slab, bytes);
@@ -866,6 +975,7 @@ int adj_setup(fvm_ctx *c)
     }
     // transposed coefficient sets and their factors, drag sensitivities
     k_adj_coef_t<<<igrid(c), 128, 0, c->stream>>>(d, d.cP, a.cPT);
+    k_adj_coef_f32<<<igrid(c), 128, 0, c->stream>>>(d, a.cPT);
     k_adj_coef_t<<<igrid(c), 128, 0, c->stream>>>(d, d.cUX, a.cXT);
     k_adj_coef_t<<<igrid(c), 128, 0, c->stream>>>(d, d.cUY, a.cYT);
     k_adj_factor<<<(a.sPT.lines + 63) / 64, 64, 0, c->stream>>>(d, a.cPT, a.sPT, 0);
@@ -893,12 +1003,23 @@ int adj_poisson_graph(fvm_ctx *c)
     if (A->pgraph) return FVM_OK;
     const Dev &d = c->d;
     const Adj &a = A->a;
-    const int per = 4, groups = 8;
+    const bool mixed = c->p.precision == FVM_MIXED;
+    const int per = mixed ? c->d.refine_sweeps : 4, groups = mixed ? std::max(1, 32 / per) : 8;
     cudaGraph_t g = nullptr;
     FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const int blocks = line_blocks((c->NJ - 1) / 2, a.sPT.NW);
     bool ok = true;
-    for (int q = 0; q < groups && ok; q++) {
+    for (int q = 0; q < groups && ok && mixed; q++) {
+        k_adj_mres<<<c->nblk_res, 256, 0, c->stream>>>(d, a, c->p.resimax, c->d.nswpp);
+        for (int it = 0; it < per && ok; it++)
+            for (int colour = 0; colour < 2; colour++)
+                ok = ok && dispatch_line(a.sPT, [&](auto m, auto nw) {
+                         k_adj_pois32<decltype(m)::value, decltype(nw)::value>
+                             <<<blocks, 128, 0, c->stream>>>(d, a, colour);
+                     });
+        k_adj_apply<<<igrid(c), 128, 0, c->stream>>>(d, a);
+    }
+    for (int q = 0; q < groups && ok && !mixed; q++) {
         for (int it = 0; it < per && ok; it++) {
             k_adj_xd<<<igrid(c), 128, 0, c->stream>>>(d, a);
             for (int colour = 0; colour < 2; colour++)

@@ -511,10 +511,16 @@ template <class S>
 __global__ void k_cfl(const __grid_constant__ S src)
 {
     const Dev &d = dev_of(src);
-    INTERIOR_IJ
-    int c = IDX(i, j);
-    double l = d.dt * (fabs(d.XIX[c] * d.U[c] + d.XIY[c] * d.V[c]) + fabs(d.ETX[c] * d.U[c] + d.ETY[c] * d.V[c]));
-    atomicMax(d.cflbits, (unsigned long long)__double_as_longlong(l));
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+    if (j > d.NJ - 1) return;   // the whole block
+    double l = 0.0;             // the CFL number is >= 0
+    if (i <= d.NI - 1) {
+        const int c = IDX(i, j);
+        l = d.dt * (fabs(d.XIX[c] * d.U[c] + d.XIY[c] * d.V[c]) + fabs(d.ETX[c] * d.U[c] + d.ETY[c] * d.V[c]));
+    }
+    // the warp's maximum (exact, order-free) goes to one atomic
+    for (int o = 16; o > 0; o >>= 1) l = fmax(l, __shfl_xor_sync(0xffffffffu, l, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(d.cflbits, (unsigned long long)__double_as_longlong(l));
 }
 
 template <class S>
@@ -525,8 +531,9 @@ __global__ void k_calc_final(const __grid_constant__ S src, double rtime, fvm_co
         rtime = *d.btime;
         out = d.bhist + (size_t)d.bctl->step * d.bctl->ncases + d.case_id;
     }
+    // one warp: each lane sums every 32nd row, then a fixed shuffle tree
     double pd = 0.0, pl = 0.0, td = 0.0, tl = 0.0, nu = 0.0;
-    for (int j = 1; j <= d.NJ - 1; j++) {
+    for (int j = 1 + (int)threadIdx.x; j <= d.NJ - 1; j += 32) {
         const double *row = d.coefrow + 8 * j;
         pd = pd - row[0];
         pl = pl - row[1];
@@ -534,6 +541,14 @@ __global__ void k_calc_final(const __grid_constant__ S src, double rtime, fvm_co
         tl = tl - row[3];
         nu = nu + row[4];
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        pd += __shfl_down_sync(0xffffffffu, pd, o);
+        pl += __shfl_down_sync(0xffffffffu, pl, o);
+        td += __shfl_down_sync(0xffffffffu, td, o);
+        tl += __shfl_down_sync(0xffffffffu, tl, o);
+        nu += __shfl_down_sync(0xffffffffu, nu, o);
+    }
+    if (threadIdx.x != 0) return;
     const double *P = d.P;
     double pg11 = 0.25 * (((P[IDX(1, 1)] + P[IDX(1, 0)]) + P[IDX(0, 1)]) + P[IDX(0, 0)]);
     out->time = rtime;
@@ -729,7 +744,7 @@ int step_after_poisson(const Tgt &t, double rtime, fvm_coeffs *dout)
     if (t.thermal) RC(predictor_sweeps(t, FVM_FIELD_T));
     LAUNCH_S(t, k_calc_rows, dim3((t.NJ + 127) / 128, 1, t.nz), 128);
     LAUNCH_S(t, k_cfl, interior_grid(t), 128);
-    LAUNCH_S(t, k_calc_final, dim3(1, 1, t.nz), 1, rtime, dout);
+    LAUNCH_S(t, k_calc_final, dim3(1, 1, t.nz), 32, rtime, dout);
     return FVM_OK;
 }
 
@@ -1033,7 +1048,7 @@ int run_calccoef(fvm_ctx *c, fvm_coeffs *out)
     fvm_coeffs *dout = coef_slot(c);
     LAUNCH_S(t, k_calc_rows, dim3((t.NJ + 127) / 128, 1, 1), 128);
     LAUNCH_S(t, k_cfl, interior_grid(t), 128);
-    LAUNCH_S(t, k_calc_final, dim3(1, 1, 1), 1, c->rtime, dout);
+    LAUNCH_S(t, k_calc_final, dim3(1, 1, 1), 32, c->rtime, dout);
     const double cl_prev = c->last.cl;   // CL_NM1 (calccoef.f90:109)
     fvm_coeffs co;
     RC(calccoef_copy(c, dout, &co));
