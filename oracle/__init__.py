@@ -230,6 +230,11 @@ class Oracle3D:
             L.o3_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
             L.o3_sgs.argtypes = [ctypes.c_void_p]
             L.o3_test_filter.argtypes = [ctypes.c_void_p, P, P]
+            L.o3_post_begin.argtypes = [ctypes.c_void_p]
+            L.o3_post_steps.argtypes = [ctypes.c_void_p]
+            L.o3_post_steps.restype = ctypes.c_int
+            L.o3_post_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, P]
+            L.o3_post_get.restype = ctypes.c_int
             L._o3_ready = True
         self.ni, self.nj, self.nk = ni, nj, nk
         if ref_a is None:
@@ -266,6 +271,24 @@ class Oracle3D:
 
     def sgs(self):
         lib().o3_sgs(self._h)
+
+    WALL_STATS = ("CF_WALL", "CP_WALL", "NU_WALL")
+
+    def post_begin(self):
+        """POST_PROCESS with IPOST=0: averaging from the next step on."""
+        lib().o3_post_begin(self._h)
+
+    def post_steps(self):
+        return lib().o3_post_steps(self._h)
+
+    def post_get(self, name):
+        """An average of POST_PROCESS with IPOST=1: a field shaped (NK+1, NJ+1, NI+1),
+        or for the wall statistics an array shaped (NK+1, NJ+1)."""
+        shape = (self.nk + 1, self.nj + 1) if name in self.WALL_STATS else (self.nk + 1, self.nj + 1, self.ni + 1)
+        out = np.zeros(shape)
+        if lib().o3_post_get(self._h, name.encode(), _dptr(out)) != 0:
+            raise KeyError(name)
+        return out
 
     def test_filter(self, a, out=None):
         """TEST_FILTER(IN, OUT) of a into the interior of out (test_filter.f90)."""

@@ -31,6 +31,10 @@ struct o3 {
     double *FW, *L[9], *DTD[3], *MAG, *UH, *VH, *WH, *TH, *MAGH, *DIN, *DOUT, *LIJ, *MIJ, *LM, *MM;
     double *EV, *EC, *SGSX, *SGSY, *SGSZ, *SGST;
     double *la, *lb, *lc, *ld, *lx, *lz, *lw, *lu, *lbb;
+    /* post-processing sums (calccoef.f90:287-306): U, V, W, P, T, UU, UV, UW, VV, VW,
+     * WW, SGS11, SGS12, SGS13, SGS22, SGS23, SGS33 */
+    double *PS[17];
+    int ipost, niter_pos;
     o3_coeffs co;
 };
 
@@ -55,6 +59,7 @@ static double **fields(o3 *o, int *count)
     F(FW); F(L[0]); F(L[1]); F(L[2]); F(L[3]); F(L[4]); F(L[5]); F(L[6]); F(L[7]); F(L[8]);
     F(DTD[0]); F(DTD[1]); F(DTD[2]); F(MAG); F(UH); F(VH); F(WH); F(TH); F(MAGH);
     F(DIN); F(DOUT); F(LIJ); F(MIJ); F(LM); F(MM); F(EV); F(EC); F(SGSX); F(SGSY); F(SGSZ); F(SGST);
+    for (int q = 0; q < 17; q++) F(PS[q]);
 #undef F
     *count = c;
     return (double **)list;
@@ -1117,6 +1122,24 @@ void o3_sgs(o3 *o)
 /* ------------------------------------------------------------------------- */
 /* CALCCOEF (calccoef.f90:9-160)                                              */
 /* ------------------------------------------------------------------------- */
+/* The post-processing block of CALCCOEF (calccoef.f90:286-307): sums over the
+ * whole array, the SGS stress as -2 nu_t S_ij of the step's model. */
+static void post_sums(o3 *o)
+{
+    o->niter_pos = o->niter_pos + 1;
+    const double *f[3] = {o->U, o->V, o->W};
+    static const int ra[] = {0, 0, 0, 1, 1, 2}, rb[] = {0, 1, 2, 1, 2, 2}, ls[] = {0, 1, 2, 4, 5, 8};
+    for (int c = 0; c < o->n; c++) {
+        o->PS[0][c] = o->PS[0][c] + o->U[c];
+        o->PS[1][c] = o->PS[1][c] + o->V[c];
+        o->PS[2][c] = o->PS[2][c] + o->W[c];
+        o->PS[3][c] = o->PS[3][c] + o->P[c];
+        o->PS[4][c] = o->PS[4][c] + o->T[c];
+        for (int q = 0; q < 6; q++) o->PS[5 + q][c] = o->PS[5 + q][c] + f[ra[q]][c] * f[rb[q]][c];
+        for (int q = 0; q < 6; q++) o->PS[11 + q][c] = o->PS[11 + q][c] - (2.0 * o->EV[c]) * o->L[ls[q]][c];
+    }
+}
+
 static void calccoef(o3 *o)
 {
     const int NI = o->NI, NJ = o->NJ, NK = o->NK;
@@ -1183,6 +1206,109 @@ static void calccoef(o3 *o)
     co->cd = co->cd_p + co->cd_v;
     co->cl = co->cl_p + co->cl_v;
     co->nu = -snu / o->sum_area;
+    if (o->ipost) post_sums(o);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Post-processing (post_process.f90:8-285, calccoef.f90:286-307)              */
+/* ------------------------------------------------------------------------- */
+void o3_post_begin(o3 *o)
+{
+    for (int q = 0; q < 17; q++) memset(o->PS[q], 0, sizeof(double) * (size_t)o->n);
+    o->niter_pos = 0;
+    o->ipost = 1;
+}
+
+int o3_post_steps(const o3 *o) { return o->niter_pos; }
+
+/* The wall statistics of the averaged fields at the wall cell (1, j, k): shear
+ * rate, wall heat flux and the pressure of the wall node, over the face's two
+ * triangles (post_process.f90:67-116), scaled as written out (:252-255). */
+static void wall_stats(const o3 *o, const double *ua, const double *va, const double *wa, const double *pa,
+                       const double *ta, int j, int k, double *cf, double *cp, double *nu)
+{
+    const double *XG = o->XG, *YG = o->YG, *ZG = o->ZG;
+    const int i = 1, c = ID(i, j, k);
+    double sh = 0.0, nus = 0.0;
+    for (int tri = 0; tri < 2; tri++) {
+        int p, q, r;
+        if (tri == 0) { p = ID(i, j, k); q = ID(i, j + 1, k); r = ID(i, j, k + 1); }
+        else { p = ID(i, j + 1, k + 1); q = ID(i, j, k + 1); r = ID(i, j, k); }
+        double A = (YG[p] * (ZG[q] - ZG[r]) + YG[q] * (ZG[r] - ZG[p])) + YG[r] * (ZG[p] - ZG[q]);
+        double B = (ZG[p] * (XG[q] - XG[r]) + ZG[q] * (XG[r] - XG[p])) + ZG[r] * (XG[p] - XG[q]);
+        double C = (XG[p] * (YG[q] - YG[r]) + XG[q] * (YG[r] - YG[p])) + XG[r] * (YG[p] - YG[q]);
+        double D = (XG[p] * (YG[q] * ZG[r] - YG[r] * ZG[q]) + XG[q] * (YG[r] * ZG[p] - YG[p] * ZG[r])) +
+                   XG[r] * (YG[p] * ZG[q] - YG[q] * ZG[p]);
+        D = -1.0 * D;
+        double dum = sqrt((A * A + B * B) + C * C);
+        double dn = fabs(((A * o->X[c] + B * o->Y[c]) + C * o->Z[c]) + D) / dum;
+        double u = ua[c], v = va[c], w = wa[c];
+        double e1 = (v * C) / dum - (w * B) / dum, e2 = (u * C) / dum - (w * A) / dum, e3 = (u * B) / dum - (v * A) / dum;
+        double dudn = sqrt((e1 * e1 + e2 * e2) + e3 * e3);
+        dudn = dudn / dn;
+        double dtdn = (ta[c] - o->p.t_wall) / dn;
+        double ar = tri == 0 ? o->AREA1[c] : o->AREA2[c];
+        double tot = o->AREA1[c] + o->AREA2[c];
+        sh = sh + (dudn * ar) / tot;
+        nus = nus + (dtdn * ar) / tot;
+    }
+    double pg = 0.125 * (((((((pa[ID(i, j, k)] + pa[ID(i, j - 1, k)]) + pa[ID(i - 1, j, k)]) + pa[ID(i - 1, j - 1, k)]) +
+                            pa[ID(i, j, k + 1)]) + pa[ID(i, j - 1, k + 1)]) + pa[ID(i - 1, j, k + 1)]) +
+                         pa[ID(i - 1, j - 1, k + 1)]);
+    *cf = (2.0 / sqrt(o->p.re)) * sh;
+    *cp = 2.0 * pg;
+    *nu = -nus;
+}
+
+/* POST_PROCESS with IPOST=1: "U_AVG".."T_AVG", the Reynolds stresses with their SGS
+ * part "UU","UV","UW","VV","VW","WW" (post_process.f90:207-212), "U_RMS".."W_RMS"
+ * (the root mean squares, :164-166), full arrays; "CF_WALL","CP_WALL","NU_WALL" at
+ * out[j + (NJ+1) k] for the wall cells.  Returns -1 for an unknown name or before
+ * any averaged step. */
+int o3_post_get(o3 *o, const char *name, double *out)
+{
+    const int n = o->n;
+    if (o->niter_pos < 1) return -1;
+    const double N = (double)o->niter_pos;
+    static const char *avg[] = {"U_AVG", "V_AVG", "W_AVG", "P_AVG", "T_AVG"};
+    for (int q = 0; q < 5; q++)
+        if (!strcmp(name, avg[q])) {
+            for (int c = 0; c < n; c++) out[c] = o->PS[q][c] / N;
+            return 0;
+        }
+    static const char *rs[] = {"UU", "UV", "UW", "VV", "VW", "WW"};
+    static const int ra[] = {0, 0, 0, 1, 1, 2}, rb[] = {0, 1, 2, 1, 2, 2};
+    for (int q = 0; q < 6; q++)
+        if (!strcmp(name, rs[q])) {
+            for (int c = 0; c < n; c++) {
+                double m = o->PS[5 + q][c] / N, a = o->PS[ra[q]][c] / N, b = o->PS[rb[q]][c] / N;
+                out[c] = (m - a * b) + o->PS[11 + q][c] / N;
+            }
+            return 0;
+        }
+    static const char *rms[] = {"U_RMS", "V_RMS", "W_RMS"};
+    static const int rq[] = {5, 8, 10};
+    for (int q = 0; q < 3; q++)
+        if (!strcmp(name, rms[q])) {
+            for (int c = 0; c < n; c++) out[c] = sqrt(o->PS[rq[q]][c] / N);
+            return 0;
+        }
+    int which = !strcmp(name, "CF_WALL") ? 0 : (!strcmp(name, "CP_WALL") ? 1 : (!strcmp(name, "NU_WALL") ? 2 : -1));
+    if (which < 0) return -1;
+    double *a[5];
+    for (int q = 0; q < 5; q++) {
+        a[q] = (double *)malloc(sizeof(double) * (size_t)n);
+        for (int c = 0; c < n; c++) a[q][c] = o->PS[q][c] / N;
+    }
+    for (int c = 0; c < o->NJ1 * (o->NK + 1); c++) out[c] = 0.0;
+    for (int k = 1; k <= o->NK - 1; k++)
+        for (int j = 1; j <= o->NJ - 1; j++) {
+            double v[3];
+            wall_stats(o, a[0], a[1], a[2], a[3], a[4], j, k, &v[0], &v[1], &v[2]);
+            out[j + o->NJ1 * k] = v[which];
+        }
+    for (int q = 0; q < 5; q++) free(a[q]);
+    return 0;
 }
 
 /* ------------------------------------------------------------------------- */

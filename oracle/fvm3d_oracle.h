@@ -72,6 +72,15 @@ const o3_coeffs *o3_last_coeffs(const o3 *o);
 void o3_sgs(o3 *o);                /* STRESS_TENSOR_DY */
 void o3_test_filter(o3 *o, const double *in, double *out);
 double *o3_array(o3 *o, const char *name);
+/* Post-processing of the LES program (no effect on the flow).
+ * o3_post_begin: POST_PROCESS with IPOST=0 (post_process.f90:8-59): the sums of
+ *   U, V, W, P, T, their six products and the six SGS stresses -2 nu_t S_ij cleared,
+ *   NITER_POS = 0; every later CALCCOEF adds the step (calccoef.f90:286-307).  The
+ *   reference also switches DTIME to DTIME_POST there; the oracle keeps its dt.
+ * o3_post_get: the averages of POST_PROCESS with IPOST=1 by name (see the .c). */
+void o3_post_begin(o3 *o);
+int o3_post_steps(const o3 *o);
+int o3_post_get(o3 *o, const char *name, double *out);
 int o3_size(const o3 *o);
 
 #ifdef __cplusplus

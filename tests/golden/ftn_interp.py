@@ -377,6 +377,9 @@ class Machine:
         self.unit_in = {}      # unit -> list of values
         self.unit_out = {}     # unit -> list of records
         self.units_open = {}
+        self.archive = []      # (unit, file name, records) of files a later OPEN replaced
+        self.drop_oob_writes = False   # skip (and log) scalar writes past an array's bounds
+        self.oob_log = []
         self.g.update(MPI_CONSTANTS)
 
     # -- declarations -----------------------------------------------------------
@@ -509,7 +512,12 @@ class Machine:
                 view = arr.a[arr.sl(specs)]
                 view[...] = conform(value, view.shape) if isinstance(value, np.ndarray) else value
             else:
-                arr.a[arr.idx(specs)] = value
+                ix = arr.idx(specs)
+                if self.drop_oob_writes and any(q < 0 or q >= n for q, n in zip(ix, arr.a.shape)):
+                    # an element past the array (undefined in the compiled program): recorded, not written
+                    self.oob_log.append((name, tuple(specs)))
+                    return
+                arr.a[ix] = value
             return
         raise ValueError(lhs)
 
@@ -802,20 +810,42 @@ def exec_stmt(M, s, env):
                 val = M.unit_in[int(unit)].pop(0)
             M.assign(tgt, val, env)
     elif t == "open":
-        m = re.match(r"^\s*(UNIT\s*=\s*)?(\d+)", s[2], re.I)
-        unit = int(m.group(2))
-        fm = re.search(r"FILE\s*=\s*'([^']*)'", s[2], re.I)
-        M.units_open[unit] = fm.group(1) if fm else None
+        m = re.match(r"^\s*(?:UNIT\s*=\s*)?([^,]+)", s[2], re.I)
+        unit = unit_number(M, m.group(1), env)
+        fm = re.search(r"FILE\s*=\s*(?:'([^']*)'|(\w+))", s[2], re.I)
+        fname = None
+        if fm:
+            fname = fm.group(1) if fm.group(1) is not None else str(M.eval(parse_expr(fm.group(2)), env)).strip()
         if re.search(r"ACCESS\s*=\s*'APPEND'", s[2], re.I):
             M.unit_out.setdefault(unit, [])
         else:   # a sequential file opened without APPEND is written from its start
+            if M.unit_out.get(unit):   # keep what the unit's previous file received
+                M.archive.append((unit, M.units_open.get(unit), M.unit_out[unit]))
             M.unit_out[unit] = []
+        M.units_open[unit] = fname
     elif t == "write":
-        unit = s[2]
-        if unit == "*" or not unit.isdigit():
+        unit = unit_number(M, s[2], env)
+        if unit is None:   # list-directed output to the screen, or an internal write
             return
         vals = [M.eval(e, env) for e in s[3]]
-        M.unit_out.setdefault(int(unit), []).append(vals)
+        M.unit_out.setdefault(unit, []).append(vals)
+
+
+def unit_number(M, text, env):
+    """The unit of an OPEN/WRITE: a literal or an integer expression such as
+    1000+RANK; None for '*' and for internal writes to character variables."""
+    t = text.strip()
+    if t == "*":
+        return None
+    if t.isdigit():
+        return int(t)
+    if "(" in t or "'" in t:
+        return None
+    try:
+        v = M.eval(parse_expr(t), env)
+    except Exception:
+        return None
+    return int(v) if isinstance(v, (int, np.integer)) else None
 
 
 def call(M, name, args, env):

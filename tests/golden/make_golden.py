@@ -118,6 +118,66 @@ CASES3D = [
 ]
 
 
+# The whole 3-D program: the loop to RTIME_MAX, POST_PROCESS (IPOST=0), the loop to
+# RTIME_END with the averaging of CALCCOEF, POST_PROCESS (IPOST=1) writing the
+# averaged, rms, Reynolds-stress and wall files; RESTART000.DAT every NITER_R steps.
+# DTIME_POST is set to DTIME (the reference switches the time step there).  After
+# its last loops POST_PROCESS writes THETA(IE+1,JE+1,KE+1), one element past the
+# array (post_process.f90:250, undefined in the compiled program): the interpreter
+# drops that write and the fixture records it.
+PROGRAM3D_CASES = [
+    dict(name="program3d_12x8x6_re3900_post", n_theta=12, n_r=8, n_z=6, skew=0.2, re=3900.0, pr=0.71, dt=0.002,
+         amp=0.05, seed=1, steps_before=3, steps_post=3, niter_r=4),
+]
+
+
+def run_program_case_3d(ref_root, c):
+    import math
+    from fvm_gb300.grid import o_grid_3d, perturbation_3d
+    g = o_grid_3d(c["n_theta"], c["n_r"], c["n_z"], lz=math.pi, dr1=0.01, skew=c["skew"])
+    dt = c["dt"]
+    over = {"NI": g.ni, "NJ": g.nj, "NK": g.nk, "NDIMJ": 1, "NDIMK": 1, "RE": c["re"], "PR": c["pr"],
+            "PE": c["re"] * c["pr"], "DTIME": dt, "DTIME_POST": dt, "RTIME_MAX": (c["steps_before"] - 0.5) * dt,
+            "RTIME_END": (c["steps_before"] + c["steps_post"] - 0.5) * dt, "NITER_R": c["niter_r"]}
+    M = F.load_program(os.path.join(ref_root, SNAPSHOT3D), FILES3D[:-1] + ["post_process.f90", "writedata.f90",
+                                                                         "main.f90"], over)
+    vals = []
+    for k in range(1, g.nk + 1):
+        for j in range(1, g.nj + 1):
+            for i in range(1, g.ni + 1):
+                vals += [float(g.xg[k, j, i]), float(g.yg[k, j, i]), float(g.zg[k, j, i])]
+    M.unit_in[10] = vals
+    main = M.subs["__MAIN__"].body
+    k_init = next(k for k, s in enumerate(main) if s[0] == "call" and s[2] == "INIT")
+    F.run_stmts(M, main[:k_init + 1], None)
+    du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, c["amp"], c["seed"])
+    for nm, dd in (("U", du), ("V", dv), ("W", dw)):
+        M.g[nm].a[...] += dd.transpose(2, 1, 0)
+    M.drop_oob_writes = True
+    F.run_stmts(M, main[k_init + 1:], None)
+    files = {name: recs for _, name, recs in M.archive}
+    for u, recs in M.unit_out.items():
+        files[M.units_open.get(u)] = recs
+
+    def numeric(recs, skip):
+        return np.array(recs[skip:], dtype=np.float64)
+
+    out = {nm: M.g[nm].a.transpose(2, 1, 0).copy() for nm in FIELDS3D}
+    out["COEFFS"] = numeric(files["NU_CD_CL.PLT"], 1)
+    out["CS"] = numeric(files["CS.PLT"], 1)          # time, sqrt of the volume-averaged coefficient
+    out["CT"] = numeric(files["CT.PLT"], 1)
+    out["AVRG"] = numeric(files["Avrg000.PLT"], 3)   # x, y, z, p, u, v, w, T at the nodes
+    out["URMS"] = numeric(files["Urms000.PLT"], 3)   # x, y, z, u_rms, v_rms, w_rms
+    out["STRS"] = numeric(files["Strs000.PLT"], 3)   # x, y, z, uu, uv, uw, vv, vw, ww
+    out["SURF"] = numeric(files["Surf000.PLT"], 3)   # x, y, z, theta, Cf, Cp, Nu at the wall cells
+    r16 = files["RESTART000.DAT"]
+    out["RESTART_HEAD"] = np.array(r16[0], dtype=np.float64)
+    out["RESTART_NL"] = np.array(r16[1::2], dtype=np.float64)
+    out["RESTART_STATE"] = np.array(r16[2::2], dtype=np.float64)
+    out["OOB_WRITES"] = np.array([list(ix) for _, ix in M.oob_log], dtype=np.int64)
+    return g, out
+
+
 def run_case_3d(ref_root, c):
     import math
     from fvm_gb300.grid import o_grid_3d, perturbation_3d
@@ -211,6 +271,18 @@ def main():
     if only3d:
         with open(os.path.join(HERE, "manifest.json")) as f:
             manifest_prog = json.load(f).get("program_cases", [])
+    manifest_prog3d = []
+    for c in ([] if only3d else PROGRAM3D_CASES):
+        t0 = time.time()
+        g, out = run_program_case_3d(ref_root, c)
+        fn = f"{c['name']}.npz"
+        np.savez_compressed(os.path.join(HERE, fn), **out)
+        manifest_prog3d.append(dict(c, file=fn, dr1=0.01, lz="pi", nswpp=20, resimax=1e-4, use_les=1,
+                                    ref_a=6.283185307))
+        print(f"{c['name']}: {time.time() - t0:.1f} s", flush=True)
+    if only3d:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest_prog3d = json.load(f).get("program_cases_3d", [])
     manifest3d = []
     if only_prog:
         with open(os.path.join(HERE, "manifest.json")) as f:
@@ -228,7 +300,8 @@ def main():
         print(f"{c['name']}: {time.time() - t0:.1f} s, {len(out['COEFFS'])} coefficient records", flush=True)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py (reference sources executed by ftn_interp)",
-                   "cases": manifest, "program_cases": manifest_prog, "cases3d": manifest3d}, f, indent=1)
+                   "cases": manifest, "program_cases": manifest_prog, "cases3d": manifest3d,
+                   "program_cases_3d": manifest_prog3d}, f, indent=1)
 
 
 if __name__ == "__main__":

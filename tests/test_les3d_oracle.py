@@ -105,3 +105,84 @@ def test_oracle_against_golden_fixtures_3d(entry):
     ref = data["COEFFS"]
     assert ref.shape == (entry["steps"], len(GOLD_COEFFS))
     np.testing.assert_allclose(np.array(recs), ref, rtol=1e-11, atol=1e-11)
+
+
+def _program3d_cases():
+    path = os.path.join(GOLD, "manifest.json")
+    if not os.path.exists(path):
+        return []
+    return json.load(open(path)).get("program_cases_3d", [])
+
+
+def _nodal(a, g):
+    """The node values the reference writes: the mean of the 8 cells around node
+    (i, j, k), i = 1..NI, j = 1..NJ, k = 1..NK (post_process.f90:120-132)."""
+    out = []
+    for k in range(1, g.nk + 1):
+        for j in range(1, g.nj + 1):
+            for i in range(1, g.ni + 1):
+                out.append(0.125 * (((((((a[k, j, i] + a[k, j - 1, i]) + a[k, j, i - 1]) + a[k, j - 1, i - 1]) +
+                                       a[k - 1, j, i]) + a[k - 1, j - 1, i]) + a[k - 1, j, i - 1]) +
+                                    a[k - 1, j - 1, i - 1]))
+    return np.array(out)
+
+
+@pytest.mark.parametrize("entry", _program3d_cases(), ids=lambda e: e["name"])
+def test_post_processing_against_the_reference_program_3d(entry, tmp_path):
+    """The whole LES program with its averaging phase: per-step coefficient and
+    dynamic-coefficient records, the averaged, rms, Reynolds-stress and wall files,
+    and the restart file, replayed by the oracle in the reference's order."""
+    from fvm_gb300 import restart
+    data = np.load(os.path.join(GOLD, entry["file"]))
+    g = o_grid_3d(entry["n_theta"], entry["n_r"], entry["n_z"], lz=math.pi, dr1=entry["dr1"], skew=entry["skew"])
+    du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, entry["amp"], entry["seed"])
+    o = oracle.Oracle3D(g.ni, g.nj, g.nk, re=entry["re"], pr=entry["pr"], dt=entry["dt"], order=oracle.O3_FAITHFUL,
+                        resimax=entry["resimax"], nswpp=entry["nswpp"], use_les=True, thermal=True,
+                        ref_a=entry["ref_a"])
+    o.set_grid(g)
+    o.init(du, dv, dw)
+    recs, cs, ct, state = [], [], [], None
+    for s in range(1, entry["steps_before"] + entry["steps_post"] + 1):
+        o.step(1)
+        c = o.coeffs()
+        recs.append([c[k] for k in GOLD_COEFFS])
+        cs.append([c["time"], math.sqrt(c["cs2"])])
+        ct.append([c["time"], math.sqrt(c["ct2"])])
+        if s % entry["niter_r"] == 0:
+            state = {nm: o.array(nm).copy() for nm in restart.STATE_3D}
+        if s == entry["steps_before"]:
+            o.post_begin()
+    assert o.post_steps() == entry["steps_post"]
+    np.testing.assert_allclose(np.array(recs), data["COEFFS"], rtol=1e-11, atol=1e-11)
+    np.testing.assert_allclose(np.array(cs), data["CS"], rtol=1e-11, atol=1e-14)
+    np.testing.assert_allclose(np.array(ct), data["CT"], rtol=1e-11, atol=1e-14)
+
+    def close(got, ref, nm):
+        assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max()), nm
+
+    for col, nm in ((3, "P_AVG"), (4, "U_AVG"), (5, "V_AVG"), (6, "W_AVG"), (7, "T_AVG")):
+        close(_nodal(o.post_get(nm), g), data["AVRG"][:, col], nm)
+    for col, nm in ((3, "U_RMS"), (4, "V_RMS"), (5, "W_RMS")):
+        close(_nodal(o.post_get(nm), g), data["URMS"][:, col], nm)
+    for col, nm in ((3, "UU"), (4, "UV"), (5, "UW"), (6, "VV"), (7, "VW"), (8, "WW")):
+        close(_nodal(o.post_get(nm), g), data["STRS"][:, col], nm)
+    for col, nm in ((4, "CF_WALL"), (5, "CP_WALL"), (6, "NU_WALL")):
+        w = o.post_get(nm)
+        close(np.array([w[k, j] for k in range(1, g.nk) for j in range(1, g.nj)]), data["SURF"][:, col], nm)
+    # the reference's one write past THETA's end is the only dropped write
+    assert data["OOB_WRITES"].tolist() == [[g.ni + 1, g.nj + 1, g.nk + 1]]
+    # RESTART000.DAT: the state of the last multiple of NITER_R, and this package's
+    # writer reproduces the reference's E24.16 fields
+    head = data["RESTART_HEAD"]
+    assert head[4] == entry["niter_r"] * (len(recs) // entry["niter_r"])
+    for q, nm in enumerate(("NLX", "NLY", "NLZ", "ADV")):
+        close(state[nm].ravel(), data["RESTART_NL"][:, q], nm)
+    for q, nm in enumerate(("U", "V", "W", "P", "T")):
+        close(state[nm].ravel(), data["RESTART_STATE"][:, q], nm)
+    path = tmp_path / "RESTART000.DAT"
+    restart.write_restart_3d(str(path), state, head[0], head[1], head[2], head[3], int(head[4]))
+    h, back = restart.read_restart_3d(str(path), g.ni, g.nj, g.nk)
+    assert h["niter_time"] == int(head[4]) and h["rtime"] == float(restart.format_e(head[3]).replace("E", "e"))
+    for nm in restart.STATE_3D:
+        ref16 = np.vectorize(lambda x: restart._num(restart.format_e(x)))(state[nm])
+        assert np.array_equal(back[nm], ref16), nm
