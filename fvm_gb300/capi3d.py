@@ -12,7 +12,8 @@ ROUTINES = ["fvm3_begin_step", "fvm3_contra_vel", "fvm3_nl", "fvm3_stress_tensor
             "fvm3_remove_grad", "fvm3_correct", "fvm3_iter_t"]
 EXPORTS = ["fvm3_default_params", "fvm3_create", "fvm3_destroy", "fvm3_last_error", "fvm3_set_grid", "fvm3_init",
            "fvm3_step", "fvm3_get_array", "fvm3_set_array", "fvm3_sgs", "fvm3_time_sweeps", "fvm3_get_stream",
-           "fvm3_iter_u", "fvm3_iter_p", "fvm3_calccoef", "fvm3_test_filter"] + ROUTINES
+           "fvm3_iter_u", "fvm3_iter_p", "fvm3_calccoef", "fvm3_test_filter", "fvm3_post_begin", "fvm3_post_get",
+           "fvm3_post_steps", "fvm3_post_end"] + ROUTINES
 
 
 class Params3(ctypes.Structure):
@@ -61,6 +62,10 @@ def load():
         L.fvm3_iter_p.argtypes = [V, D, ctypes.POINTER(ctypes.c_int)]
         L.fvm3_calccoef.argtypes = [V, ctypes.POINTER(Coeffs3)]
         L.fvm3_test_filter.argtypes = [V, D, D]
+        L.fvm3_post_begin.argtypes = [V]
+        L.fvm3_post_end.argtypes = [V]
+        L.fvm3_post_steps.argtypes = [V, ctypes.POINTER(ctypes.c_int)]
+        L.fvm3_post_get.argtypes = [V, ctypes.c_char_p, D]
         _ready = True
     return L
 
@@ -159,6 +164,28 @@ class Context3:
         dst = np.zeros(self.n) if out is None else self._arr(out).copy()
         self._ok(self.L.fvm3_test_filter(self.h, _dp(src), _dp(dst)))
         return dst.reshape(self.shape)
+
+    WALL_STATS = ("CF_WALL", "CP_WALL", "NU_WALL")
+
+    def post_begin(self):
+        """POST_PROCESS with IPOST=0: averaging from the next step on."""
+        self._ok(self.L.fvm3_post_begin(self.h))
+
+    def post_end(self):
+        self._ok(self.L.fvm3_post_end(self.h))
+
+    def post_steps(self) -> int:
+        n = ctypes.c_int()
+        self._ok(self.L.fvm3_post_steps(self.h, ctypes.byref(n)))
+        return n.value
+
+    def post_get(self, name) -> np.ndarray:
+        """An average of POST_PROCESS with IPOST=1: a field shaped like the state, or
+        for the wall statistics an array shaped (NK+1, NJ+1)."""
+        shape = (self.nk + 1, self.nj + 1) if name in self.WALL_STATS else self.shape
+        out = np.zeros(shape)
+        self._ok(self.L.fvm3_post_get(self.h, name.encode(), _dp(out)))
+        return out
 
     def sgs(self) -> dict:
         c = Coeffs3()

@@ -1523,6 +1523,30 @@ __global__ void __launch_bounds__(1024) k3_calc_final(D3 d, double rtime, double
 
 }  // namespace f3
 
+namespace f3 {
+// The post-processing block of CALCCOEF (calccoef.f90:286-307): the step added to
+// the sums of U, V, W, P, T (ps 0..4), of the six velocity products (5..10) and of
+// the SGS stresses -2 nu_t S_ij of the step's model (11..16), over the whole array.
+__global__ void k3_post_acc(D3 d, double *ps)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    const size_t n = d.n;
+    const double u = d.U[c], v = d.V[c], w = d.W[c], f[3] = {u, v, w};
+    ps[c] += u;
+    ps[n + c] += v;
+    ps[2 * n + c] += w;
+    ps[3 * n + c] += d.P[c];
+    ps[4 * n + c] += d.T[c];
+    const int ra[6] = {0, 0, 0, 1, 1, 2}, rb[6] = {0, 1, 2, 1, 2, 2}, ls[6] = {0, 1, 2, 4, 5, 8};
+#pragma unroll
+    for (int q = 0; q < 6; q++) ps[(5 + q) * n + c] += f[ra[q]] * f[rb[q]];
+    const double ev2 = 2.0 * d.EV[c];
+#pragma unroll
+    for (int q = 0; q < 6; q++) ps[(11 + q) * n + c] -= ev2 * d.L[ls[q]][c];
+}
+}  // namespace f3
+
 // ---------------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------------
@@ -1541,6 +1565,9 @@ struct fvm3_ctx {
     int pgraph_iters = 0;
     fvm3_coeffs last{};
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    // post-processing: 17 sum arrays on the device, allocated on first use
+    double *post = nullptr;
+    int ipost = 0, niter_pos = 0;
 };
 
 namespace f3 {
@@ -2011,6 +2038,10 @@ int calccoef(fvm3_ctx *c)   // CALCCOEF kernels; the record is read by read_coef
     k3_cfl<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1, c->NK - 1), 128, 0, c->stream>>>(d);
     k3_wall<<<dim3((c->NJ + 127) / 128, c->NK - 1, 2), 128, 0, c->stream>>>(d);
     k3_calc_final<<<1, 1024, 0, c->stream>>>(d, c->rtime, c->sum_area);
+    if (c->ipost && c->post) {
+        k3_post_acc<<<g_lin(c), 256, 0, c->stream>>>(d, c->post);
+        c->niter_pos += 1;
+    }
     F3CHECK(c);
     return FVM_OK;
 }
@@ -2135,6 +2166,7 @@ int fvm3_destroy(fvm3_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->pgraph) cudaGraphExecDestroy(c->pgraph);
     if (c->slab) cudaFree(c->slab);
+    if (c->post) cudaFree(c->post);
     if (c->h_pctl) cudaFreeHost(c->h_pctl);
     if (c->ev_a) cudaEventDestroy(c->ev_a);
     if (c->ev_b) cudaEventDestroy(c->ev_b);
@@ -2306,6 +2338,133 @@ int fvm3_test_filter(fvm3_ctx *c, const double *in, double *out)
     F3CHECK(c);
     F3CUDA(c, cudaMemcpyAsync(out, d.MM, bytes, cudaMemcpyDeviceToHost, c->stream));
     F3CUDA(c, cudaStreamSynchronize(c->stream));
+    return FVM_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Post-processing (post_process.f90:8-285)
+// ---------------------------------------------------------------------------------
+int fvm3_post_begin(fvm3_ctx *c)
+{
+    if (!c) return FVM_ERR_ARG;
+    if (!c->grid_set) return f3::bad3(c, "fvm3_set_grid has not been called");
+    const size_t bytes = sizeof(double) * 17 * size_t(c->n);
+    if (!c->post) F3CUDA(c, cudaMalloc(&c->post, bytes));
+    F3CUDA(c, cudaMemsetAsync(c->post, 0, bytes, c->stream));
+    F3CUDA(c, cudaStreamSynchronize(c->stream));
+    c->niter_pos = 0;
+    c->ipost = 1;
+    return FVM_OK;
+}
+
+int fvm3_post_end(fvm3_ctx *c)
+{
+    if (!c) return FVM_ERR_ARG;
+    c->ipost = 0;
+    return FVM_OK;
+}
+
+int fvm3_post_steps(fvm3_ctx *c, int *steps)
+{
+    if (!c || !steps) return FVM_ERR_ARG;
+    *steps = c->niter_pos;
+    return FVM_OK;
+}
+
+namespace {
+int down(fvm3_ctx *c, const double *dev, std::vector<double> &h)
+{
+    h.resize(c->n);
+    F3CUDA(c, cudaMemcpyAsync(h.data(), dev, sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->stream));
+    return FVM_OK;
+}
+}  // namespace
+
+int fvm3_post_get(fvm3_ctx *c, const char *name, double *out)
+{
+    if (!c || !name || !out) return f3::bad3(c, "null argument");
+    if (!c->post || c->niter_pos < 1) return f3::bad3(c, "no post-processing steps have been averaged");
+    const int n = c->n;
+    const double N = (double)c->niter_pos;
+    const double *ps = c->post;
+    auto sum = [&](int q, std::vector<double> &h) { return down(c, ps + size_t(q) * n, h); };
+    auto sync = [&]() -> int { F3CUDA(c, cudaStreamSynchronize(c->stream)); return FVM_OK; };
+    static const char *avg[] = {"U_AVG", "V_AVG", "W_AVG", "P_AVG", "T_AVG"};
+    static const char *rs[] = {"UU", "UV", "UW", "VV", "VW", "WW"};
+    static const char *rms[] = {"U_RMS", "V_RMS", "W_RMS"};
+    static const int ra[] = {0, 0, 0, 1, 1, 2}, rb[] = {0, 1, 2, 1, 2, 2}, rq[] = {5, 8, 10};
+    std::vector<double> a, b, m, sg;
+    for (int q = 0; q < 5; q++)
+        if (!std::strcmp(name, avg[q])) {   // post_process.f90:61-65
+            F3RC(sum(q, a));
+            F3RC(sync());
+            for (int e = 0; e < n; e++) out[e] = a[e] / N;
+            return FVM_OK;
+        }
+    for (int q = 0; q < 6; q++)
+        if (!std::strcmp(name, rs[q])) {   // post_process.f90:156-167, 207-212
+            F3RC(sum(ra[q], a));
+            F3RC(sum(rb[q], b));
+            F3RC(sum(5 + q, m));
+            F3RC(sum(11 + q, sg));
+            F3RC(sync());
+            for (int e = 0; e < n; e++) out[e] = (m[e] / N - (a[e] / N) * (b[e] / N)) + sg[e] / N;
+            return FVM_OK;
+        }
+    for (int q = 0; q < 3; q++)
+        if (!std::strcmp(name, rms[q])) {   // post_process.f90:164-166
+            F3RC(sum(rq[q], m));
+            F3RC(sync());
+            for (int e = 0; e < n; e++) out[e] = std::sqrt(m[e] / N);
+            return FVM_OK;
+        }
+    const int which = !std::strcmp(name, "CF_WALL") ? 0 : (!std::strcmp(name, "CP_WALL") ? 1 : (!std::strcmp(name, "NU_WALL") ? 2 : -1));
+    if (which < 0) return f3::bad3(c, "unknown post-processing array name");
+    // wall statistics of the averaged fields (post_process.f90:67-116, 252-255)
+    const f3::D3 &d = c->d;
+    std::vector<double> f[5], XG, YG, ZG, X, Y, Z, A1, A2;
+    for (int q = 0; q < 5; q++) F3RC(sum(q, f[q]));
+    F3RC(down(c, d.XG, XG)); F3RC(down(c, d.YG, YG)); F3RC(down(c, d.ZG, ZG));
+    F3RC(down(c, d.X, X)); F3RC(down(c, d.Y, Y)); F3RC(down(c, d.Z, Z));
+    F3RC(down(c, d.AREA1, A1)); F3RC(down(c, d.AREA2, A2));
+    F3RC(sync());
+    for (int q = 0; q < 5; q++)
+        for (int e = 0; e < n; e++) f[q][e] = f[q][e] / N;
+    const int NI1 = c->NI + 1, NJ1 = c->NJ + 1;
+    auto id = [&](int i, int j, int k) { return i + NI1 * (j + NJ1 * k); };
+    for (int e = 0; e < NJ1 * (c->NK + 1); e++) out[e] = 0.0;
+    for (int k = 1; k <= c->NK - 1; k++)
+        for (int j = 1; j <= c->NJ - 1; j++) {
+            const int i = 1, cc = id(i, j, k);
+            double sh = 0.0, nus = 0.0;
+            for (int tri = 0; tri < 2; tri++) {
+                int p, q, r;
+                if (tri == 0) { p = id(i, j, k); q = id(i, j + 1, k); r = id(i, j, k + 1); }
+                else { p = id(i, j + 1, k + 1); q = id(i, j, k + 1); r = id(i, j, k); }
+                const double A = (YG[p] * (ZG[q] - ZG[r]) + YG[q] * (ZG[r] - ZG[p])) + YG[r] * (ZG[p] - ZG[q]);
+                const double B = (ZG[p] * (XG[q] - XG[r]) + ZG[q] * (XG[r] - XG[p])) + ZG[r] * (XG[p] - XG[q]);
+                const double C = (XG[p] * (YG[q] - YG[r]) + XG[q] * (YG[r] - YG[p])) + XG[r] * (YG[p] - YG[q]);
+                double D = (XG[p] * (YG[q] * ZG[r] - YG[r] * ZG[q]) + XG[q] * (YG[r] * ZG[p] - YG[p] * ZG[r])) +
+                           XG[r] * (YG[p] * ZG[q] - YG[q] * ZG[p]);
+                D = -1.0 * D;
+                const double dum = std::sqrt((A * A + B * B) + C * C);
+                const double dn = std::fabs(((A * X[cc] + B * Y[cc]) + C * Z[cc]) + D) / dum;
+                const double u = f[0][cc], v = f[1][cc], w = f[2][cc];
+                const double e1 = (v * C) / dum - (w * B) / dum, e2 = (u * C) / dum - (w * A) / dum,
+                             e3 = (u * B) / dum - (v * A) / dum;
+                const double dudn = std::sqrt((e1 * e1 + e2 * e2) + e3 * e3) / dn;
+                const double dtdn = (f[4][cc] - c->p.t_wall) / dn;
+                const double ar = tri == 0 ? A1[cc] : A2[cc], tot = A1[cc] + A2[cc];
+                sh = sh + (dudn * ar) / tot;
+                nus = nus + (dtdn * ar) / tot;
+            }
+            const std::vector<double> &P = f[3];
+            const double pg = 0.125 * (((((((P[id(i, j, k)] + P[id(i, j - 1, k)]) + P[id(i - 1, j, k)]) +
+                                          P[id(i - 1, j - 1, k)]) + P[id(i, j, k + 1)]) + P[id(i, j - 1, k + 1)]) +
+                                        P[id(i - 1, j, k + 1)]) + P[id(i - 1, j - 1, k + 1)]);
+            const double v3[3] = {(2.0 / std::sqrt(c->p.re)) * sh, 2.0 * pg, -nus};
+            out[j + NJ1 * k] = v3[which];
+        }
     return FVM_OK;
 }
 

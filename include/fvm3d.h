@@ -96,6 +96,23 @@ int fvm3_calccoef(struct fvm3_ctx *ctx, fvm3_coeffs *out);
  * host array in into the interior of the host array out (its other entries are
  * left as passed).  Needs the grid only. */
 int fvm3_test_filter(struct fvm3_ctx *ctx, const double *in, double *out);
+/* Post-processing of the LES program (post_process.f90, calccoef.f90:286-307):
+ *   fvm3_post_begin  POST_PROCESS with IPOST=0: the sums cleared, NITER_POS = 0;
+ *                    from the next step on every CALCCOEF (fvm3_step,
+ *                    fvm3_calccoef) adds U, V, W, P, T, their six products and the
+ *                    six SGS stresses -2 nu_t S_ij on the device.  The reference
+ *                    also switches DTIME to DTIME_POST there; dt is left unchanged.
+ *   fvm3_post_get    POST_PROCESS with IPOST=1, by name: "U_AVG","V_AVG","W_AVG",
+ *                    "P_AVG","T_AVG"; the Reynolds stresses with their SGS part
+ *                    "UU","UV","UW","VV","VW","WW"; the root mean squares
+ *                    "U_RMS","V_RMS","W_RMS" (full arrays); the wall statistics
+ *                    "CF_WALL","CP_WALL","NU_WALL" at out[j + (NJ+1) k] for the
+ *                    wall cells (j, k), (NJ+1)*(NK+1) doubles.
+ *   fvm3_post_steps  NITER_POS;  fvm3_post_end: averaging off. */
+int fvm3_post_begin(struct fvm3_ctx *ctx);
+int fvm3_post_get(struct fvm3_ctx *ctx, const char *name, double *out);
+int fvm3_post_steps(struct fvm3_ctx *ctx, int *steps);
+int fvm3_post_end(struct fvm3_ctx *ctx);
 /* Named arrays ("U","V","W","P","T","NLX","NLY","NLZ","ADV","DJAC","SGS_X",...). */
 int fvm3_get_array(struct fvm3_ctx *ctx, const char *name, double *out);
 int fvm3_set_array(struct fvm3_ctx *ctx, const char *name, const double *in);

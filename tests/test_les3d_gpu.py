@@ -151,3 +151,28 @@ def test_mixed_tracks_fp64_on_a_wall_resolved_grid():
     for nm in ("U", "V", "W", "T"):
         assert rel_l2(out[capi.MIXED][0][nm], out[capi.FP64][0][nm]) <= 1e-3, nm
     assert abs(out[capi.MIXED][1] - out[capi.FP64][1]) <= 1e-3 * abs(out[capi.FP64][1])
+
+
+POST3 = ("U_AVG", "V_AVG", "W_AVG", "P_AVG", "T_AVG", "UU", "UV", "UW", "VV", "VW", "WW", "U_RMS", "V_RMS", "W_RMS",
+         "CF_WALL", "CP_WALL", "NU_WALL")
+
+
+def test_post_processing_matches_the_restatement():
+    """Time averages, Reynolds stresses with their SGS part, rms and wall statistics
+    of the averaging phase (fvm3_post_*) against the restatement in the same order
+    (both stop the Poisson iteration at the same sweep cap)."""
+    g, o, ctx = _case(resimax=1e-30, nswpp=400)
+    for s in range(2):
+        o.step(1)
+        ctx.step(1)
+    o.post_begin()
+    ctx.post_begin()
+    for s in range(3):
+        o.step(1)
+        ctx.step(1)
+    assert ctx.post_steps() == o.post_steps() == 3
+    for nm in POST3:
+        assert rel_l2(ctx.post_get(nm), o.post_get(nm)) <= 1e-9, nm
+    ctx.post_end()
+    ctx.step(1)
+    assert ctx.post_steps() == 3
