@@ -564,9 +564,8 @@ def run_les3d_bench(args):
                    "poisson": f"red-black I-line GS to scaled-L1 {w['resimax']:g}, cap NSWPP={w['nswpp']}",
                    "sweeps_per_step": res["mixed"]["sweeps"],
                    "precision": f"mixed: FP32 red-black Poisson sweeps in FP64 refinement every "
-                                f"{w['refine_sweeps']} sweeps; DIF and predictor cross terms in FP32 on "
-                                "FP64 differences; metrics, residuals, SGS model, predictor line "
-                                "solves and state FP64",
+                                f"{w['refine_sweeps']} sweeps; metrics, residuals, predictor, SGS model and "
+                                "state FP64",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "256 MiB buffer written between timed steps (outside the events)"},
         "fp64": {"value": fp64_value, "ms_per_step": res["fp64"]["ms"] / args.steps,

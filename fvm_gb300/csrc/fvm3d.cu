@@ -697,8 +697,10 @@ __global__ void k3_explicit(D3 d, int thermal)
     if (thermal) d.ADV[c] = nl3(d, d.T_N, c, i, j, k);
 }
 
-// DIF of the four fields; T = float in the mixed path (the stencil sums in FP32 on
-// FP64 differences, the result stored in FP64).
+// DIF of the four fields.  T is the arithmetic type of the sums; both paths use
+// double: on GB300 each double-to-float conversion issues on the FP64 pipe, so an
+// FP32 sum of FP64 inputs is slower than the FP64 sum (measured: 911 us against
+// 625 us per launch at 256x192x48).
 template <class T>
 __global__ void k3_dif(D3 d, int thermal)
 {
@@ -769,8 +771,8 @@ __global__ void k3_ghost(D3 d, double *phi, const double *ff, int kind)
 
 // Right-hand side of one AF sweep (iter_u.f90:44-100, iter_T.f90): the split's
 // twelve cross terms of phi, the sweep's source, and the BC folding of BCU/BCT.
-// T: arithmetic type of the cross terms (float in the mixed path, on FP64
-// differences); the source terms are always FP64.
+// T: arithmetic type of the cross terms, double in both paths (a float version
+// pays one FP64-pipe conversion per input on GB300 and is no faster).
 template <class T>
 __global__ void k3_af_rhs(D3 d, Coef3 cf, int split, int kind, const double *phi, const double *phin,
                           const double *ina, const double *inb, const double *inc, const double *ind,
@@ -1787,8 +1789,8 @@ int predictor(fvm3_ctx *c, int kind, double *phi, const double *phin, const doub
     D3 &d = c->d;
     const int base = kind == 2 ? 3 : 0;
     for (int split = 0; split < 3; split++) {
-        auto rhs = c->p.precision == FVM_MIXED ? k3_af_rhs<float> : k3_af_rhs<double>;
-        rhs<<<g_int(c), B_INT, 0, c->stream>>>(d, d.cf[base + split], split, kind, phi, phin, ina, inb, inc, ind, ff);
+        k3_af_rhs<double><<<g_int(c), B_INT, 0, c->stream>>>(d, d.cf[base + split], split, kind, phi, phin, ina, inb,
+                                                             inc, ind, ff);
         k3_ghost<<<dim3((c->NJ + 1 + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, phi, ff, kind);
         F3RC(halo(c, {phi}));
         F3RC(line(c, base + split, d.SU, phi, 0));
@@ -1966,8 +1968,7 @@ int nl_all(fvm3_ctx *c)   // main.f90:50-57
 
 int dif_all(fvm3_ctx *c)   // main.f90:72-75
 {
-    auto dif = c->p.precision == FVM_MIXED ? k3_dif<float> : k3_dif<double>;
-    dif<<<g_int(c), B_INT, 0, c->stream>>>(c->d, c->d.thermal);
+    k3_dif<double><<<g_int(c), B_INT, 0, c->stream>>>(c->d, c->d.thermal);
     F3CHECK(c);
     return FVM_OK;
 }

@@ -32,11 +32,9 @@ typedef struct fvm3_params {
     int res_every;         /* Poisson residual every k-th sweep */
     double ref_a;          /* reference area of the force coefficients (REF_A) */
     int precision;         /* FVM_FP64, or FVM_MIXED: FP32 red-black Poisson sweeps on the
-                              correction inside FP64 residual refinement; DIF and the
-                              predictor's cross terms summed in FP32 from FP64 differences;
-                              metrics, residuals, the SGS model (its Leonard term cancels
-                              to ~1e-6 of its operands), the predictor's line solves and
-                              the state stay FP64 */
+                              correction inside FP64 residual refinement; everything else
+                              (metrics, residuals, predictor, the SGS model, whose Leonard
+                              term cancels to ~1e-6 of its operands, and the state) FP64 */
     int refine_sweeps;     /* MIXED: FP32 sweeps per FP64 residual */
     int device;
 } fvm3_params;
