@@ -44,7 +44,10 @@ struct D3 {
     double *XG, *YG, *ZG, *X, *Y, *Z;
     double *XIX, *XIY, *XIZ, *ETX, *ETY, *ETZ, *ZTX, *ZTY, *ZTZ, *DJAC;
     double *Q11, *Q12, *Q13, *Q22, *Q23, *Q33;
-    double *JQ12, *JQ13, *JQ23;   // Q12*DJAC, Q13*DJAC, Q23*DJAC (the cross-term weights)
+    double *JQ12, *JQ13, *JQ23;   // Q12*DJAC, Q13*DJAC, Q23*DJAC
+    // The twelve-term cross derivatives as weights of the 12 edge neighbours (see
+    // k3_cw): CW for DIF_DIAGONAL / ITER_P, CWA[s] for the AF split s of ITER_U/T.
+    double *CW[12], *CWA[3][12];
     double *DE, *DW, *DN, *DS, *DT, *DB, *THETA, *AREA1, *AREA2, *FW;
     double *MD[9];          // metric derivatives (scratch of the setup)
     // state
@@ -382,6 +385,38 @@ __global__ void k3_coef_p(D3 d, Coef3 cf)
     cf.AN[c] = -d.DN[c]; cf.AS[c] = -d.DS[c]; cf.AT[c] = -d.DT[c]; cf.AB[c] = -d.DB[c];
 }
 
+// Weights of the 12 edge neighbours of an interior cell for products A12..A32 given
+// by prod(pair, cell): pair 0 A12 (the I direction of the (i,j) pair), 1 A21,
+// 2 A13, 3 A31, 4 A23, 5 A32.  set < 0: DIF_DIAGONAL / ITER_P (A_xy = J*Q_xy,
+// symmetric); set = s: AF split s, A_xy = (J m_x) m_y with the split's metrics.
+__global__ void k3_cw(D3 d, int set)
+{
+    CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
+    const int c = ID3(i, j, k);
+    const double *J = d.DJAC;
+    const double *m[3] = {set == 0 ? d.XIX : (set == 1 ? d.XIY : d.XIZ), set == 0 ? d.ETX : (set == 1 ? d.ETY : d.ETZ),
+                          set == 0 ? d.ZTX : (set == 1 ? d.ZTY : d.ZTZ)};
+    auto prod = [&](int x, int y, int cell) {   // A_xy at cell (x, y in 0..2)
+        if (set < 0) {
+            const int q = x + y;   // 1: Q12, 2: Q13, 3: Q23
+            return (q == 1 ? d.JQ12 : (q == 2 ? d.JQ13 : d.JQ23))[cell];
+        }
+        return (J[cell] * m[x][cell]) * m[y][cell];
+    };
+    const int sj = d.NI1, sk = d.NI1 * d.NJ1;
+    const int st[3] = {1, sj, sk};
+    const int px[3] = {0, 0, 1}, py[3] = {1, 2, 2};   // the three pairs (i,j), (i,k), (j,k)
+    double *const *W = set < 0 ? d.CW : d.CWA[set];
+#pragma unroll
+    for (int pr = 0; pr < 3; pr++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int a = (q & 2) ? -1 : 1, b = (q & 1) ? -1 : 1, x = px[pr], y = py[pr];
+            const double w = prod(x, y, c + a * st[x]) + prod(y, x, c + b * st[y]);
+            W[4 * pr + q][c] = (0.25 * (double)(a * b)) * w;
+        }
+}
+
 // Line families: 0 = I lines (transverse j,k), 1 = J lines (i,k), 2 = K lines (i,j).
 struct Fam {
     int n, lines;
@@ -644,41 +679,44 @@ __device__ __forceinline__ double nl3(const D3 &d, const double *in, int c, int 
                     d.WT[c] * (in[ID3(i, j, k + 1)] + p)) - d.WB[c] * (in[ID3(i, j, k - 1)] + p)));
 }
 
-// DIF_DIAGONAL (dif_diagonal.f90:13-32): twelve cross terms with Q*J.  T is the
-// arithmetic type of the weighted sum (double, or float in the mixed path's DIF);
-// the differences of f are formed in FP64 first.
-template <class T = double>
-__device__ __forceinline__ T cross12(const D3 &d, const double *f, int i, int j, int k)
+// The 12 edge neighbours of a cell: (+-1,+-1,0), (+-1,0,+-1), (0,+-1,+-1) in the
+// order (+,+), (+,-), (-,+), (-,-) of each pair.
+__device__ __forceinline__ int edge_off(const D3 &d, int e)
 {
-#define F3(a, b, c) f[ID3(i + (a), j + (b), k + (c))]
-#define G3(Q, a, b, c) T(d.J##Q[ID3(i + (a), j + (b), k + (c))])
-#define DF(x) T(x)
-    T s = G3(Q12, 1, 0, 0) * DF(F3(1, 1, 0) - F3(1, -1, 0));
-    s = s - G3(Q12, -1, 0, 0) * DF(F3(-1, 1, 0) - F3(-1, -1, 0));
-    s = s + G3(Q13, 1, 0, 0) * DF(F3(1, 0, 1) - F3(1, 0, -1));
-    s = s - G3(Q13, -1, 0, 0) * DF(F3(-1, 0, 1) - F3(-1, 0, -1));
-    s = s + G3(Q12, 0, 1, 0) * DF(F3(1, 1, 0) - F3(-1, 1, 0));
-    s = s - G3(Q12, 0, -1, 0) * DF(F3(1, -1, 0) - F3(-1, -1, 0));
-    s = s + G3(Q23, 0, 1, 0) * DF(F3(0, 1, 1) - F3(0, 1, -1));
-    s = s - G3(Q23, 0, -1, 0) * DF(F3(0, -1, 1) - F3(0, -1, -1));
-    s = s + G3(Q13, 0, 0, 1) * DF(F3(1, 0, 1) - F3(-1, 0, 1));
-    s = s - G3(Q13, 0, 0, -1) * DF(F3(1, 0, -1) - F3(-1, 0, -1));
-    s = s + G3(Q23, 0, 0, 1) * DF(F3(0, 1, 1) - F3(0, -1, 1));
-    s = s - G3(Q23, 0, 0, -1) * DF(F3(0, 1, -1) - F3(0, -1, -1));
-#undef F3
-#undef G3
-#undef DF
-    return T(0.25) * s;
+    const int sj = d.NI1, sk = d.NI1 * d.NJ1;
+    const int a = (e & 2) ? -1 : 1, b = (e & 1) ? -1 : 1;
+    if (e < 4) return a + b * sj;
+    if (e < 8) return a + b * sk;
+    return a * sj + b * sk;
+}
+
+// A twelve-term cross derivative (dif_diagonal.f90:13-32, iter_u.f90:61-84) is
+// linear in the 12 edge neighbours: with products A_xy at the cells, the
+// neighbour (a, b, 0) carries 0.25 s(a) s(b) (A_12(i+a) + A_21(j+b)), and likewise
+// for the (i,k) and (j,k) pairs.  The weights depend on the geometry only and are
+// formed once (k3_cw); a cross term is then 12 fused multiply-adds.
+__device__ __forceinline__ double cross_w(const D3 &d, double *const *W, const double *f, int c)
+{
+    double s = 0.0;
+#pragma unroll
+    for (int e = 0; e < 12; e++) s = fma(W[e][c], f[c + edge_off(d, e)], s);
+    return s;
+}
+
+// DIF_DIAGONAL with the J*Q weights
+__device__ __forceinline__ double cross12(const D3 &d, const double *f, int i, int j, int k)
+{
+    return cross_w(d, d.CW, f, ID3(i, j, k));
 }
 
 template <class T>
 __device__ __forceinline__ double dif3(const D3 &d, const double *in, int c, int i, int j, int k)
 {   // DIF (dif.f90:15-23)
     const double p = in[c];
-    return (double)(T(1) * ((((((T(d.DE[c]) * T(in[ID3(i + 1, j, k)] - p) + T(d.DW[c]) * T(in[ID3(i - 1, j, k)] - p)) +
-                                T(d.DN[c]) * T(in[ID3(i, j + 1, k)] - p)) + T(d.DS[c]) * T(in[ID3(i, j - 1, k)] - p)) +
-                              T(d.DT[c]) * T(in[ID3(i, j, k + 1)] - p)) + T(d.DB[c]) * T(in[ID3(i, j, k - 1)] - p)) +
-                            cross12<T>(d, in, i, j, k)));
+    return 1.0 * ((((((d.DE[c] * (in[ID3(i + 1, j, k)] - p) + d.DW[c] * (in[ID3(i - 1, j, k)] - p)) +
+                      d.DN[c] * (in[ID3(i, j + 1, k)] - p)) + d.DS[c] * (in[ID3(i, j - 1, k)] - p)) +
+                    d.DT[c] * (in[ID3(i, j, k + 1)] - p)) + d.DB[c] * (in[ID3(i, j, k - 1)] - p)) +
+                  cross12(d, in, i, j, k));
 }
 
 // NL of the four fields (shifting the previous values to *_NM1), DIF of the four
@@ -781,26 +819,7 @@ __global__ void k3_af_rhs(D3 d, Coef3 cf, int split, int kind, const double *phi
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *J = d.DJAC;
-    const double *m1 = split == 0 ? d.XIX : (split == 1 ? d.XIY : d.XIZ);
-    const double *m2 = split == 0 ? d.ETX : (split == 1 ? d.ETY : d.ETZ);
-    const double *m3 = split == 0 ? d.ZTX : (split == 1 ? d.ZTY : d.ZTZ);
-#define F3(a, b, cc) phi[ID3(i + (a), j + (b), k + (cc))]
-#define P3(ma, mb, a, b, cc) ((T(J[ID3(i + (a), j + (b), k + (cc))]) * T(ma[ID3(i + (a), j + (b), k + (cc))])) * T(mb[ID3(i + (a), j + (b), k + (cc))]))
-    T s = P3(m1, m2, 1, 0, 0) * T(F3(1, 1, 0) - F3(1, -1, 0));
-    s = s - P3(m1, m2, -1, 0, 0) * T(F3(-1, 1, 0) - F3(-1, -1, 0));
-    s = s + P3(m1, m3, 1, 0, 0) * T(F3(1, 0, 1) - F3(1, 0, -1));
-    s = s - P3(m1, m3, -1, 0, 0) * T(F3(-1, 0, 1) - F3(-1, 0, -1));
-    s = s + P3(m2, m1, 0, 1, 0) * T(F3(1, 1, 0) - F3(-1, 1, 0));
-    s = s - P3(m2, m1, 0, -1, 0) * T(F3(1, -1, 0) - F3(-1, -1, 0));
-    s = s + P3(m2, m3, 0, 1, 0) * T(F3(0, 1, 1) - F3(0, 1, -1));
-    s = s - P3(m2, m3, 0, -1, 0) * T(F3(0, -1, 1) - F3(0, -1, -1));
-    s = s + P3(m3, m1, 0, 0, 1) * T(F3(1, 0, 1) - F3(-1, 0, 1));
-    s = s - P3(m3, m1, 0, 0, -1) * T(F3(1, 0, -1) - F3(-1, 0, -1));
-    s = s + P3(m3, m2, 0, 0, 1) * T(F3(0, 1, 1) - F3(0, -1, 1));
-    s = s - P3(m3, m2, 0, 0, -1) * T(F3(0, 1, -1) - F3(0, -1, -1));
-#undef F3
-#undef P3
-    const double dd = (double)(T(0.25) * s);
+    const double dd = cross_w(d, d.CWA[split], phi, c);
     const double rek = kind == 2 ? d.pe : d.re;
     const double r = ((2.0 * rek) * J[c]) / d.dt;
     double su;
@@ -1624,6 +1643,9 @@ void carve(Bump &b, fvm3_ctx *c)
                        &d.MM, &d.EV, &d.EC};
     for (auto p : full) *p = b.take(n);
     for (int q = 0; q < 9; q++) d.L[q] = b.take(n);
+    for (int e = 0; e < 12; e++) d.CW[e] = b.take(n);
+    for (int sp = 0; sp < 3; sp++)
+        for (int e = 0; e < 12; e++) d.CWA[sp][e] = b.take(n);
     for (int q = 0; q < 9; q++) d.MD[q] = d.L[q];   // metric derivatives live in the strain arrays at setup
     double **perjk[] = {&d.FFU, &d.FFV, &d.FFW, &d.FFT};
     for (auto p : perjk) *p = b.take(jk);
@@ -1753,6 +1775,7 @@ int setup_grid(fvm3_ctx *c)
         k3_coef_af<<<g_int(c), B_INT, 0, st>>>(d, d.cf[3 + s], s, d.pe);
     }
     k3_coef_p<<<g_int(c), B_INT, 0, st>>>(d, d.cf[6]);
+    for (int set = -1; set < 3; set++) k3_cw<<<g_int(c), B_INT, 0, st>>>(d, set);
     k3_coef_f32<<<g_lin(c), 256, 0, st>>>(d);
     F3CHECK(c);
     for (int s = 0; s < 7; s++) {
