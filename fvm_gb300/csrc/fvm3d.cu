@@ -610,10 +610,9 @@ __global__ void __launch_bounds__(128) k3_line(D3 d, LineSys s, Coef3 cf, const 
         v[q] = 0.0;
         if (active && e < n) {
             const int c = g.base + e * g.stride;
-            const double cp = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(c1[c], phi[c + g.o1]), __dmul_rn(c2[c], phi[c + g.o2])),
-                                                  __dmul_rn(c3[c], phi[c + g.o3])),
-                                        __dmul_rn(c4[c], phi[c + g.o4]));
-            v[q] = __dadd_rn(cp, SU[c]);
+            // the four transverse couplings and the source as fused multiply-adds
+            v[q] = fma(c1[c], phi[c + g.o1], fma(c2[c], phi[c + g.o2], fma(c3[c], phi[c + g.o3],
+                                                                             fma(c4[c], phi[c + g.o4], SU[c]))));
         }
     }
     fvm::to_chunks<double, M, NW>(v, sm[gib], t);
@@ -878,8 +877,9 @@ __global__ void k3_bcp(D3 d, int check_done)
     P[ID3(d.NI, j, k)] = (3.0 * P[ID3(d.NI - 1, j, k)] - 3.0 * P[ID3(d.NI - 2, j, k)]) + P[ID3(d.NI - 3, j, k)];
 }
 
-// Deterministic two-level sum of three values (block tree, then the last block).
-__device__ bool grid_sum3(const D3 &d, double &a, double &b, double &e, double *sh, bool &last, unsigned *ticket)
+// Block sum of three values (warp shuffle trees, then the warps in order; thread 0
+// holds the result).
+__device__ __forceinline__ void block_sum3(double &a, double &b, double &e, double *sh)
 {
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(0xffffffffu, a, o);
@@ -887,32 +887,45 @@ __device__ bool grid_sum3(const D3 &d, double &a, double &b, double &e, double *
         e += __shfl_down_sync(0xffffffffu, e, o);
     }
     const int wid = threadIdx.x / WARP, lane = threadIdx.x & 31, nw = blockDim.x / WARP;
+    __syncthreads();   // sh may hold an earlier round's values
     if (lane == 0) { sh[3 * wid] = a; sh[3 * wid + 1] = b; sh[3 * wid + 2] = e; }
     __syncthreads();
     if (threadIdx.x == 0) {
         double x = 0.0, y = 0.0, z = 0.0;
         for (int w = 0; w < nw; w++) { x += sh[3 * w]; y += sh[3 * w + 1]; z += sh[3 * w + 2]; }
-        d.partial[4 * blockIdx.x] = x;
-        d.partial[4 * blockIdx.x + 1] = y;
-        d.partial[4 * blockIdx.x + 2] = z;
+        a = x;
+        b = y;
+        e = z;
+    }
+}
+
+// Deterministic two-level sum of three values over the grid: each block's sum goes
+// to `partial`; the last block to arrive sums the partials with all its threads
+// (a fixed strided assignment, then the block tree).  Returns true in the last
+// block, whose thread 0 holds the sums.
+__device__ bool grid_sum3(const D3 &d, double &a, double &b, double &e, double *sh, bool &last, unsigned *ticket)
+{
+    block_sum3(a, b, e, sh);
+    if (threadIdx.x == 0) {
+        d.partial[4 * blockIdx.x] = a;
+        d.partial[4 * blockIdx.x + 1] = b;
+        d.partial[4 * blockIdx.x + 2] = e;
         __threadfence();
         unsigned t = atomicInc(ticket, gridDim.x - 1);
         last = (t == gridDim.x - 1);
     }
     __syncthreads();
     if (!last) return false;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        double x = 0.0, y = 0.0, z = 0.0;
-        for (unsigned q = 0; q < gridDim.x; q++) {
-            x += ((volatile double *)d.partial)[4 * q];
-            y += ((volatile double *)d.partial)[4 * q + 1];
-            z += ((volatile double *)d.partial)[4 * q + 2];
-        }
-        a = x;
-        b = y;
-        e = z;
+    __threadfence();
+    a = 0.0;
+    b = 0.0;
+    e = 0.0;
+    for (unsigned q = threadIdx.x; q < gridDim.x; q += blockDim.x) {
+        a += ((volatile double *)d.partial)[4 * q];
+        b += ((volatile double *)d.partial)[4 * q + 1];
+        e += ((volatile double *)d.partial)[4 * q + 2];
     }
+    block_sum3(a, b, e, sh);
     return true;
 }
 
@@ -1915,7 +1928,7 @@ int sgs(fvm3_ctx *c)
 {
     D3 &d = c->d;
     cudaStream_t st = c->stream;
-    k3_strain<<<dim3((c->NI + 1 + 127) / 128, c->NJ - 1, c->NK - 1), 128, 0, st>>>(d);
+    k3_strain<<<dim3((c->NI + 1 + 31) / 32, (c->NJ - 1 + 3) / 4, c->NK - 1), B_INT, 0, st>>>(d);
     F3RC(halo(c, {d.L[0], d.L[1], d.L[2], d.L[3], d.L[4], d.L[5], d.L[6], d.L[7], d.L[8], d.DTD[0], d.DTD[1],
                   d.DTD[2]}));
     k3_mag<<<g_lin(c), 256, 0, st>>>(d);
