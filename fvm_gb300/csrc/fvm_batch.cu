@@ -374,7 +374,7 @@ int fvm_batch_tiles(const fvm_batch *b, int *tiles)
 int fvm_batch_set_tiles(fvm_batch *b, const int *tiles)
 {
     if (!b || !tiles) return FVM_ERR_ARG;
-    auto ok = [](int nw, int m) { return (nw == 1 || nw == 2 || nw == 4) && m >= 1 && m <= 4; };
+    auto ok = [](int nw, int m) { return fvm::tile_supported(nw, m); };
     if (!ok(tiles[0], tiles[1]) || !ok(tiles[2], tiles[3])) return berr(b, "invalid line tile");
     return apply_tiles(b, tiles[0], tiles[1], tiles[2], tiles[3]);
 }
@@ -407,8 +407,9 @@ int fvm_batch_autotune(fvm_batch *b, int sweeps, int *tiles, double *ms)
     for (int fam = 0; fam < 2 && rc == FVM_OK; fam++) {
         const int n = fam == 0 ? nr : nt;
         for (int nw = 1; nw <= 4 && rc == FVM_OK; nw *= 2) {
-            const int m = (n + 32 * nw - 1) / (32 * nw);
-            if (m > 4) continue;
+            int m = (n + 32 * nw - 1) / (32 * nw);
+            while (m <= 12 && !fvm::tile_supported(nw, m)) m++;   // the smallest instantiated tile that covers n
+            if (!fvm::tile_supported(nw, m)) continue;
             int tl[4] = {best[0], best[1], best[2], best[3]};
             tl[2 * fam] = nw;
             tl[2 * fam + 1] = m;

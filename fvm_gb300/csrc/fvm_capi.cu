@@ -36,9 +36,9 @@ int check_params(const fvm_params *p, std::string &why)
     if (p->precision != FVM_FP64 && p->precision != FVM_MIXED) { why = "unknown precision"; return FVM_ERR_ARG; }
     auto tile_ok = [&](int nw, int m, int n, const char *fam) {
         if (nw == 0 && m == 0) return true;
-        if ((nw != 1 && nw != 2 && nw != 4) || m < 1 || m > 4 || 32 * nw * m < n) {
-            why = std::string("invalid ") + fam + " line tile (warps 1, 2 or 4; 1..4 elements per thread; "
-                  "32*warps*elements >= line length)";
+        if (!fvm::tile_supported(nw, m) || 32 * nw * m < n) {
+            why = std::string("invalid ") + fam + " line tile (warps 1, 2 or 4; 1..4 elements per thread, also "
+                  "6, 8, 12 with one warp and 6, 8 with two; 32*warps*elements >= line length)";
             return false;
         }
         return true;

@@ -486,11 +486,12 @@ template <typename F>
 inline bool dispatch_line(const LineSys &s, F &&f)
 {
     using std::integral_constant;
-    switch (s.NW * 8 + s.M) {
+    switch (s.NW * 32 + s.M) {
 #define FVM_LCASE(NWV, MV) \
-    case NWV * 8 + MV: f(integral_constant<int, MV>(), integral_constant<int, NWV>()); return true;
+    case NWV * 32 + MV: f(integral_constant<int, MV>(), integral_constant<int, NWV>()); return true;
         FVM_LCASE(1, 1) FVM_LCASE(1, 2) FVM_LCASE(1, 3) FVM_LCASE(1, 4)
-        FVM_LCASE(2, 1) FVM_LCASE(2, 2) FVM_LCASE(2, 3) FVM_LCASE(2, 4)
+        FVM_LCASE(1, 6) FVM_LCASE(1, 8) FVM_LCASE(1, 12)
+        FVM_LCASE(2, 1) FVM_LCASE(2, 2) FVM_LCASE(2, 3) FVM_LCASE(2, 4) FVM_LCASE(2, 6) FVM_LCASE(2, 8)
         FVM_LCASE(4, 1) FVM_LCASE(4, 2) FVM_LCASE(4, 3) FVM_LCASE(4, 4)
 #undef FVM_LCASE
     default: return false;
@@ -513,6 +514,16 @@ inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, cudaSt
     cfg.attrs = at;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+// Line tiles with a kernel instantiation: NW warps per line (1, 2, 4) and M
+// elements per thread (1..4; also 6, 8, 12 for one warp and 6, 8 for two).
+inline bool tile_supported(int nw, int m)
+{
+    if (nw == 4) return m >= 1 && m <= 4;
+    if (nw == 2) return (m >= 1 && m <= 4) || m == 6 || m == 8;
+    if (nw == 1) return (m >= 1 && m <= 4) || m == 6 || m == 8 || m == 12;
+    return false;
 }
 
 // Blocks of 128 threads needed for `lines` line groups of NW warps.

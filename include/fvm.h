@@ -66,9 +66,10 @@ typedef struct fvm_params {
                               cell (I,J), zero on row/column 1, as the reference's whole-array DD
                               operand evaluates (dif.f90:15-23, iter_p.f90:27-30); 0: cell (I,J) */
     /* Line tiles (0 = automatic): warps per line group (1, 2 or 4) and elements per
-       thread (1..4) of the radial lines (NI-1 unknowns: Poisson and first predictor
-       factor) and of the circumferential lines (NJ-1 unknowns: second factor);
-       32 * warps * elements must cover the line.  Set both of a family or neither. */
+       thread (1..4; also 6, 8, 12 with one warp, 6, 8 with two) of the radial lines
+       (NI-1 unknowns: Poisson and first predictor factor) and of the circumferential
+       lines (NJ-1 unknowns: second factor); 32 * warps * elements must cover the
+       line.  Set both of a family or neither. */
     int tile_r_warps, tile_r_m, tile_t_warps, tile_t_m;
 } fvm_params;
 
