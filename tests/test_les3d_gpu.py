@@ -132,15 +132,16 @@ def test_test_filter_matches_the_restatement():
 
 def test_mixed_tracks_fp64_on_a_wall_resolved_grid():
     """On a grid with the first radial spacing of the LES configuration (0.001 D)
-    the mixed path stays close to the FP64 path over several steps.  Both stop the
-    Poisson iteration at the same sweep cap, so they differ by the unconverged
-    remainders (~1e-5), not by the precision of the stencils."""
+    the mixed path stays close to the FP64 path over several steps, and the flow
+    stays bounded (the coefficient averaged over the volume, as the reference).
+    Both stop the Poisson iteration at the same sweep cap, so they differ by the
+    unconverged remainders (~1e-5), not by the precision of the stencils."""
     g = o_grid_3d(64, 48, 16, lz=np.pi, dr1=0.001)
     du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, 0.05, 0)
     out = {}
     for prec in (capi.FP64, capi.MIXED):
         p = capi3d.default_params(ni=g.ni, nj=g.nj, nk=g.nk, re=3900.0, dt=0.002, resimax=1e-12, nswpp=200,
-                                  use_les=1, les_zavg=1, thermal=1, res_every=4, ref_a=np.pi, precision=prec,
+                                  use_les=1, les_zavg=0, thermal=1, res_every=4, ref_a=np.pi, precision=prec,
                                   refine_sweeps=20)
         ctx = capi3d.Context3(p)
         ctx.set_grid(g)
@@ -151,6 +152,9 @@ def test_mixed_tracks_fp64_on_a_wall_resolved_grid():
     for nm in ("U", "V", "W", "T"):
         assert rel_l2(out[capi.MIXED][0][nm], out[capi.FP64][0][nm]) <= 1e-3, nm
     assert abs(out[capi.MIXED][1] - out[capi.FP64][1]) <= 1e-3 * abs(out[capi.FP64][1])
+    # bounded flow through the impulsive start (|u| stays near 2, the drag coefficient
+    # swings within tens while the capped Poisson iteration settles)
+    assert np.abs(out[capi.FP64][0]["U"]).max() < 3.0 and abs(out[capi.FP64][1]) < 50.0
 
 
 POST3 = ("U_AVG", "V_AVG", "W_AVG", "P_AVG", "T_AVG", "UU", "UV", "UW", "VV", "VW", "WW", "U_RMS", "V_RMS", "W_RMS",
