@@ -22,7 +22,8 @@ class Params3(ctypes.Structure):
                 ("tin", ctypes.c_double), ("t_wall", ctypes.c_double), ("resimax", ctypes.c_double),
                 ("nswpp", ctypes.c_int), ("use_les", ctypes.c_int), ("les_zavg", ctypes.c_int),
                 ("thermal", ctypes.c_int), ("res_every", ctypes.c_int), ("ref_a", ctypes.c_double),
-                ("precision", ctypes.c_int), ("refine_sweeps", ctypes.c_int), ("device", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("refine_sweeps", ctypes.c_int), ("device", ctypes.c_int),
+                ("tile_i_warps", ctypes.c_int), ("tile_i_m", ctypes.c_int)]
 
 
 class Coeffs3(ctypes.Structure):

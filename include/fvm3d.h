@@ -37,6 +37,10 @@ typedef struct fvm3_params {
                               term cancels to ~1e-6 of its operands, and the state) FP64 */
     int refine_sweeps;     /* MIXED: FP32 sweeps per FP64 residual */
     int device;
+    int tile_i_warps, tile_i_m;   /* tile of the I lines (Poisson and first AF sweep), 0 = automatic:
+                                     warps per line group (1, 2, 4) and elements per thread
+                                     (1..4; also 6, 8, 12 with one warp, 6, 8 with two);
+                                     32 * warps * elements must cover NI-1 */
 } fvm3_params;
 
 typedef struct fvm3_coeffs {
