@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfvm_gb300.so")
 SOURCES = ["fvm_setup.cu", "fvm_step.cu", "fvm_mixed.cu", "fvm_capi.cu", "fvm_static.cu", "fvm_batch.cu", "fvm_adjoint.cu", "fvm3d.cu", "fvm_post.cu"]
-HEADERS = ["fvm_internal.cuh", "fvm_ops.cuh", os.path.join("..", "..", "include", "fvm.h"),
+HEADERS = ["fvm_internal.cuh", "fvm_ops.cuh", "fvm_df.cuh", os.path.join("..", "..", "include", "fvm.h"),
            os.path.join("..", "..", "include", "fvm3d.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

@@ -18,14 +18,20 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
+#include "fvm_df.cuh"
 #include "fvm_internal.cuh"
 #include "../../include/fvm3d.h"
 
 namespace f3 {
 
+using fvm::dd;
+using fvm::ld;
 using fvm::LineSys;
+using fvm::scale2;
+using fvm::to_d;
 using fvm::PCtl;
 using fvm::WARP;
 
@@ -39,6 +45,11 @@ struct Coef3 {
 struct D3 {
     int NI, NJ, NK, NI1, NJ1, n, nblk;
     double re, pe, dt, rdt, tin, t_wall, pi, resimax, ref_a;
+    double r2re_dt, r2pe_dt;   // 2 Re / dt and 2 Pe / dt (double-float AF right-hand sides)
+    // Mixed path: the arrays read by the double-float kernels have (hi, lo) float
+    // pair shadows at the constant element offset sh (dfl = 1); see carve().
+    long long sh;
+    int dfl;
     int nswpp, res_every, les_zavg, thermal, refine_sweeps;
     // geometry
     double *XG, *YG, *ZG, *X, *Y, *Z;
@@ -87,6 +98,31 @@ __device__ __forceinline__ int kw(const D3 &d, int k) { return k == 0 ? d.NK - 1
     const int k = blockIdx.z + (k0);                                                                \
     if (i > (i1) || j > (j1) || k > (k1)) return;
 
+// The (hi, lo) shadow of an array of the shadowed group (mixed path only).
+__device__ __forceinline__ float2 *shadow(const D3 &d, const double *p)
+{
+    return reinterpret_cast<float2 *>(const_cast<double *>(p) + d.sh);
+}
+// Element c of a shadowed array in arithmetic type T: the double itself (FP64 path)
+// or its shadow pair (mixed path; no split on the load).
+template <class T>
+__device__ __forceinline__ T lds(const D3 &d, const double *p, int c);
+template <>
+__device__ __forceinline__ double lds<double>(const D3 &, const double *p, int c) { return p[c]; }
+template <>
+__device__ __forceinline__ dd lds<dd>(const D3 &d, const double *p, int c)
+{
+    const float2 v = shadow(d, p)[c];
+    return dd(v.x, v.y);
+}
+// Store into a shadowed array: the double, and in the mixed path its shadow too.
+__device__ __forceinline__ void sts(const D3 &, double *p, int c, double v) { p[c] = v; }
+__device__ __forceinline__ void sts(const D3 &d, double *p, int c, dd v)
+{
+    p[c] = fvm::dd_join(v);
+    shadow(d, p)[c] = make_float2(v.hi, v.lo);
+}
+
 // ---------------------------------------------------------------------------------
 // Periodic copy of MPI_X (mpi_x.f90:25-51): J planes for every K, then K planes for
 // every J (two launches).  Up to 16 arrays per launch.
@@ -115,6 +151,17 @@ __global__ void k3_halo_k(D3 d, Arrs A)
         double *a = A.a[q];
         a[ID3(i, j, 0)] = a[ID3(i, j, d.NK - 1)];
         a[ID3(i, j, d.NK)] = a[ID3(i, j, 1)];
+    }
+}
+
+// The shadows of up to 16 shadowed arrays over the whole array (mixed path).
+__global__ void k3_shadow(D3 d, Arrs A)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    for (int q = 0; q < A.n; q++) {
+        const dd v = fvm::dd_split(A.a[q][c]);
+        shadow(d, A.a[q])[c] = make_float2(v.hi, v.lo);
     }
 }
 
@@ -670,12 +717,17 @@ __global__ void k3_fluxes(D3 d, int with_div)
     if (with_div) d.DIVDT[c] = d.rdt * (((((ue - uw) + vn) - vs) + wt) - wb);
 }
 
-__device__ __forceinline__ double nl3(const D3 &d, const double *in, int c, int i, int j, int k)
+template <class T>
+__device__ __forceinline__ T nl3(const D3 &d, const double *in, int c, int i, int j, int k)
 {   // NL (nl.f90:23-31)
-    const double p = in[c];
-    return 0.5 * ((((((d.UE[c] * (in[ID3(i + 1, j, k)] + p) - d.UW[c] * (in[ID3(i - 1, j, k)] + p)) +
-                      d.VN[c] * (in[ID3(i, j + 1, k)] + p)) - d.VS[c] * (in[ID3(i, j - 1, k)] + p)) +
-                    d.WT[c] * (in[ID3(i, j, k + 1)] + p)) - d.WB[c] * (in[ID3(i, j, k - 1)] + p)));
+    const T p = lds<T>(d, in, c);
+    return scale2(((((ld<T>(d.UE[c]) * (lds<T>(d, in, ID3(i + 1, j, k)) + p) -
+                      ld<T>(d.UW[c]) * (lds<T>(d, in, ID3(i - 1, j, k)) + p)) +
+                     ld<T>(d.VN[c]) * (lds<T>(d, in, ID3(i, j + 1, k)) + p)) -
+                    ld<T>(d.VS[c]) * (lds<T>(d, in, ID3(i, j - 1, k)) + p)) +
+                   ld<T>(d.WT[c]) * (lds<T>(d, in, ID3(i, j, k + 1)) + p)) -
+                      ld<T>(d.WB[c]) * (lds<T>(d, in, ID3(i, j, k - 1)) + p),
+                  0.5f);
 }
 
 // The 12 edge neighbours of a cell: (+-1,+-1,0), (+-1,0,+-1), (0,+-1,+-1) in the
@@ -694,32 +746,38 @@ __device__ __forceinline__ int edge_off(const D3 &d, int e)
 // neighbour (a, b, 0) carries 0.25 s(a) s(b) (A_12(i+a) + A_21(j+b)), and likewise
 // for the (i,k) and (j,k) pairs.  The weights depend on the geometry only and are
 // formed once (k3_cw); a cross term is then 12 fused multiply-adds.
-__device__ __forceinline__ double cross_w(const D3 &d, double *const *W, const double *f, int c)
+template <class T = double>
+__device__ __forceinline__ T cross_w(const D3 &d, double *const *W, const double *f, int c)
 {
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
-    for (int e = 0; e < 12; e++) s = fma(W[e][c], f[c + edge_off(d, e)], s);
+    for (int e = 0; e < 12; e++) s = fma(lds<T>(d, W[e], c), lds<T>(d, f, c + edge_off(d, e)), s);
     return s;
 }
 
 // DIF_DIAGONAL with the J*Q weights
-__device__ __forceinline__ double cross12(const D3 &d, const double *f, int i, int j, int k)
+template <class T = double>
+__device__ __forceinline__ T cross12(const D3 &d, const double *f, int i, int j, int k)
 {
-    return cross_w(d, d.CW, f, ID3(i, j, k));
+    return cross_w<T>(d, d.CW, f, ID3(i, j, k));
 }
 
 template <class T>
-__device__ __forceinline__ double dif3(const D3 &d, const double *in, int c, int i, int j, int k)
+__device__ __forceinline__ T dif3(const D3 &d, const double *in, int c, int i, int j, int k)
 {   // DIF (dif.f90:15-23)
-    const double p = in[c];
-    return 1.0 * ((((((d.DE[c] * (in[ID3(i + 1, j, k)] - p) + d.DW[c] * (in[ID3(i - 1, j, k)] - p)) +
-                      d.DN[c] * (in[ID3(i, j + 1, k)] - p)) + d.DS[c] * (in[ID3(i, j - 1, k)] - p)) +
-                    d.DT[c] * (in[ID3(i, j, k + 1)] - p)) + d.DB[c] * (in[ID3(i, j, k - 1)] - p)) +
-                  cross12(d, in, i, j, k));
+    const T p = lds<T>(d, in, c);
+    return (((((lds<T>(d, d.DE, c) * (lds<T>(d, in, ID3(i + 1, j, k)) - p) +
+                lds<T>(d, d.DW, c) * (lds<T>(d, in, ID3(i - 1, j, k)) - p)) +
+               lds<T>(d, d.DN, c) * (lds<T>(d, in, ID3(i, j + 1, k)) - p)) +
+              lds<T>(d, d.DS, c) * (lds<T>(d, in, ID3(i, j - 1, k)) - p)) +
+             lds<T>(d, d.DT, c) * (lds<T>(d, in, ID3(i, j, k + 1)) - p)) +
+            lds<T>(d, d.DB, c) * (lds<T>(d, in, ID3(i, j, k - 1)) - p)) +
+           cross12<T>(d, in, i, j, k);
 }
 
 // NL of the four fields (shifting the previous values to *_NM1), DIF of the four
-// fields, P_SOURCE (p_source.f90:14-42).
+// fields, P_SOURCE (p_source.f90:14-42).  T: double (FP64 path) or dd (mixed path).
+template <class T>
 __global__ void k3_explicit(D3 d, int thermal)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
@@ -728,27 +786,28 @@ __global__ void k3_explicit(D3 d, int thermal)
     d.NLY_NM1[c] = d.NLY[c];
     d.NLZ_NM1[c] = d.NLZ[c];
     d.ADV_NM1[c] = d.ADV[c];
-    d.NLX[c] = nl3(d, d.U_N, c, i, j, k);
-    d.NLY[c] = nl3(d, d.V_N, c, i, j, k);
-    d.NLZ[c] = nl3(d, d.W_N, c, i, j, k);
-    if (thermal) d.ADV[c] = nl3(d, d.T_N, c, i, j, k);
+    d.NLX[c] = to_d(nl3<T>(d, d.U_N, c, i, j, k));
+    d.NLY[c] = to_d(nl3<T>(d, d.V_N, c, i, j, k));
+    d.NLZ[c] = to_d(nl3<T>(d, d.W_N, c, i, j, k));
+    if (thermal) d.ADV[c] = to_d(nl3<T>(d, d.T_N, c, i, j, k));
 }
 
-// DIF of the four fields.  T is the arithmetic type of the sums; both paths use
-// double: on GB300 each double-to-float conversion issues on the FP64 pipe, so an
-// FP32 sum of FP64 inputs is slower than the FP64 sum (measured: 911 us against
-// 625 us per launch at 256x192x48).
+// DIF of the four fields.  An FP32 sum of the FP64 inputs is no option on GB300
+// (each double-to-float conversion issues on the FP64 pipe: measured 911 us against
+// 625 us per launch at 256x192x48); the mixed path sums in double-float, whose loads
+// split the doubles on the integer pipe.
 template <class T>
 __global__ void k3_dif(D3 d, int thermal)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
-    d.DIFX[c] = dif3<T>(d, d.U_N, c, i, j, k);
-    d.DIFY[c] = dif3<T>(d, d.V_N, c, i, j, k);
-    d.DIFZ[c] = dif3<T>(d, d.W_N, c, i, j, k);
-    if (thermal) d.DIFT[c] = dif3<T>(d, d.T_N, c, i, j, k);
+    d.DIFX[c] = to_d(dif3<T>(d, d.U_N, c, i, j, k));
+    d.DIFY[c] = to_d(dif3<T>(d, d.V_N, c, i, j, k));
+    d.DIFZ[c] = to_d(dif3<T>(d, d.W_N, c, i, j, k));
+    if (thermal) d.DIFT[c] = to_d(dif3<T>(d, d.T_N, c, i, j, k));
 }
 
+template <class T>
 __global__ void k3_psource(D3 d)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
@@ -757,11 +816,18 @@ __global__ void k3_psource(D3 d)
               t = ID3(i, j, k + 1), b = ID3(i, j, k - 1);
     const double *M1[3] = {d.XIX, d.XIY, d.XIZ}, *M2[3] = {d.ETX, d.ETY, d.ETZ}, *M3[3] = {d.ZTX, d.ZTY, d.ZTZ};
     double *out[3] = {d.S_U, d.S_V, d.S_W};
+    const T Je = lds<T>(d, J, e), Jw = lds<T>(d, J, w), Jn = lds<T>(d, J, nn), Js = lds<T>(d, J, s), Jt = lds<T>(d, J, t),
+            Jb = lds<T>(d, J, b);
+    const T Pe = ld<T>(in[e]), Pw = ld<T>(in[w]), Pn = ld<T>(in[nn]), Ps = ld<T>(in[s]), Pt = ld<T>(in[t]),
+            Pb = ld<T>(in[b]);
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        double a = (((((J[e] * M1[q][e]) * in[e] - (J[w] * M1[q][w]) * in[w]) + (J[nn] * M2[q][nn]) * in[nn]) -
-                     (J[s] * M2[q][s]) * in[s]) + (J[t] * M3[q][t]) * in[t]) - (J[b] * M3[q][b]) * in[b];
-        out[q][c] = -0.5 * a;
+        const T a = (((((Je * lds<T>(d, M1[q], e)) * Pe - (Jw * lds<T>(d, M1[q], w)) * Pw) +
+                       (Jn * lds<T>(d, M2[q], nn)) * Pn) -
+                      (Js * lds<T>(d, M2[q], s)) * Ps) +
+                     (Jt * lds<T>(d, M3[q], t)) * Pt) -
+                    (Jb * lds<T>(d, M3[q], b)) * Pb;
+        out[q][c] = to_d(scale2(a, -0.5f));
     }
 }
 
@@ -808,8 +874,8 @@ __global__ void k3_ghost(D3 d, double *phi, const double *ff, int kind)
 
 // Right-hand side of one AF sweep (iter_u.f90:44-100, iter_T.f90): the split's
 // twelve cross terms of phi, the sweep's source, and the BC folding of BCU/BCT.
-// T: arithmetic type of the cross terms, double in both paths (a float version
-// pays one FP64-pipe conversion per input on GB300 and is no faster).
+// T: double (FP64 path) or dd (mixed path, where 2 Re J / dt is J times the
+// precomputed 2 Re / dt instead of a division per cell).
 template <class T>
 __global__ void k3_af_rhs(D3 d, Coef3 cf, int split, int kind, const double *phi, const double *phin,
                           const double *ina, const double *inb, const double *inc, const double *ind,
@@ -818,22 +884,25 @@ __global__ void k3_af_rhs(D3 d, Coef3 cf, int split, int kind, const double *phi
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *J = d.DJAC;
-    const double dd = cross_w(d, d.CWA[split], phi, c);
+    const T cr = cross_w<T>(d, d.CWA[split], phi, c);
     const double rek = kind == 2 ? d.pe : d.re;
-    const double r = ((2.0 * rek) * J[c]) / d.dt;
-    double su;
+    T r;
+    if constexpr (std::is_same<T, double>::value) r = ((2.0 * rek) * J[c]) / d.dt;
+    else r = lds<T>(d, J, c) * ld<T>(kind == 2 ? d.r2pe_dt : d.r2re_dt);
+    T su;
     if (split == 0) {
-        su = (r * phin[c] - (3.0 * rek) * ina[c]) + (1.0 * rek) * inb[c];
-        su = su + inc[c];
-        if (ind) su = su + (2.0 * rek) * ind[c];
-        su = su + dd;
+        const T re1 = ld<T>(rek);
+        su = (r * lds<T>(d, phin, c) - (T(3) * re1) * ld<T>(ina[c])) + re1 * ld<T>(inb[c]);
+        su = su + ld<T>(inc[c]);
+        if (ind) su = su + scale2(re1, 2.0f) * ld<T>(ind[c]);
+        su = su + cr;
     } else {
-        su = r * phi[c] + dd;
+        su = r * lds<T>(d, phi, c) + cr;
     }
     const double uf = kind == 2 ? d.t_wall : 0.0;
-    if (i == 1) su = su + (2.0 * cf.awall[JK(j, k)]) * uf;
-    if (i == d.NI - 1) su = su + (2.0 * cf.afar[JK(j, k)]) * ff[JK(j, k)];
-    d.SU[c] = su;
+    if (i == 1) su = su + scale2(ld<T>(cf.awall[JK(j, k)]), 2.0f) * ld<T>(uf);
+    if (i == d.NI - 1) su = su + scale2(ld<T>(cf.afar[JK(j, k)]), 2.0f) * ld<T>(ff[JK(j, k)]);
+    d.SU[c] = to_d(su);
 }
 
 // u += sign * dt * S / J (main.f90:84-86, 104-106)
@@ -1092,27 +1161,27 @@ namespace f3 {
 // ---------------------------------------------------------------------------------
 // Dynamic Smagorinsky model (stress_tensor_dy.f90:20-735, test_filter.f90:13-21)
 // ---------------------------------------------------------------------------------
-// The model's stencils are templates over the arithmetic type T: double for the
-// FP64 path; float for the mixed path, where the filters, the filtered strain and
-// the Germano terms run in FP32 on FP64 inputs (GB300's FP64 rate makes the 27-point
-// product filters ALU-bound in FP64) and the results are stored in FP64.
+// The model's stencils are templates over the arithmetic type T and are instantiated
+// with double in both precision modes: the Leonard term filt(u_i u_j) - û_i û_j is
+// a difference of O(1) numbers that is ~1e-6 on a wall-resolved grid, so FP32
+// arithmetic leaves it with ~10 % error.
 template <class T>
 __device__ __forceinline__ T dxi(const D3 &d, const double *m, const double *f, int i, int j, int k)
 {
     const int c = ID3(i, j, k);
-    if (i == 0) return (T(2) * T(m[c])) * (T(f[ID3(1, j, k)]) - T(f[c]));
-    if (i == d.NI) return (T(2) * T(m[c])) * (T(f[c]) - T(f[ID3(d.NI - 1, j, k)]));
-    return T(m[c]) * (T(f[ID3(i + 1, j, k)]) - T(f[ID3(i - 1, j, k)]));
+    if (i == 0) return scale2(lds<T>(d, m, c), 2.0f) * (lds<T>(d, f, ID3(1, j, k)) - lds<T>(d, f, c));
+    if (i == d.NI) return scale2(lds<T>(d, m, c), 2.0f) * (lds<T>(d, f, c) - lds<T>(d, f, ID3(d.NI - 1, j, k)));
+    return lds<T>(d, m, c) * (lds<T>(d, f, ID3(i + 1, j, k)) - lds<T>(d, f, ID3(i - 1, j, k)));
 }
 template <class T>
 __device__ __forceinline__ T deta(const D3 &d, const double *m, const double *f, int i, int j, int k)
 {
-    return T(m[ID3(i, j, k)]) * (T(f[ID3(i, j + 1, k)]) - T(f[ID3(i, j - 1, k)]));
+    return lds<T>(d, m, ID3(i, j, k)) * (lds<T>(d, f, ID3(i, j + 1, k)) - lds<T>(d, f, ID3(i, j - 1, k)));
 }
 template <class T>
 __device__ __forceinline__ T dzeta(const D3 &d, const double *m, const double *f, int i, int j, int k)
 {
-    return T(m[ID3(i, j, k)]) * (T(f[ID3(i, j, k + 1)]) - T(f[ID3(i, j, k - 1)]));
+    return lds<T>(d, m, ID3(i, j, k)) * (lds<T>(d, f, ID3(i, j, k + 1)) - lds<T>(d, f, ID3(i, j, k - 1)));
 }
 
 // Strain-rate components S11..S33 of (u,v,w) (0.5 / 0.25 times the index-difference
@@ -1129,8 +1198,9 @@ __device__ void strain3(const D3 &d, const double *u, const double *v, const dou
         for (int b = a; b < 3; b++) {
             T val;
             if (a == b) {
-                val = T(0.5) * ((dxi<T>(d, M1[a], F[a], i, j, k) + deta<T>(d, M2[a], F[a], i, j, k)) +
-                                dzeta<T>(d, M3[a], F[a], i, j, k));
+                val = scale2((dxi<T>(d, M1[a], F[a], i, j, k) + deta<T>(d, M2[a], F[a], i, j, k)) +
+                                 dzeta<T>(d, M3[a], F[a], i, j, k),
+                             0.5f);
             } else {
                 T s = dxi<T>(d, M1[b], F[a], i, j, k);
                 s = s + deta<T>(d, M2[b], F[a], i, j, k);
@@ -1138,7 +1208,7 @@ __device__ void strain3(const D3 &d, const double *u, const double *v, const dou
                 s = s + dxi<T>(d, M1[a], F[b], i, j, k);
                 s = s + deta<T>(d, M2[a], F[b], i, j, k);
                 s = s + dzeta<T>(d, M3[a], F[b], i, j, k);
-                val = T(0.25) * s;
+                val = scale2(s, 0.25f);
             }
             S[3 * a + b] = val;
             S[3 * b + a] = val;
@@ -1146,7 +1216,8 @@ __device__ void strain3(const D3 &d, const double *u, const double *v, const dou
     if (t)
 #pragma unroll
         for (int q = 0; q < 3; q++)
-            G[q] = T(0.5) * ((dxi<T>(d, M1[q], t, i, j, k) + deta<T>(d, M2[q], t, i, j, k)) + dzeta<T>(d, M3[q], t, i, j, k));
+            G[q] = scale2((dxi<T>(d, M1[q], t, i, j, k) + deta<T>(d, M2[q], t, i, j, k)) + dzeta<T>(d, M3[q], t, i, j, k),
+                          0.5f);
 }
 
 template <class T>
@@ -1158,26 +1229,28 @@ __device__ __forceinline__ T sq9(const T *S)
     return s;
 }
 
+template <class T>
 __global__ void k3_strain(D3 d)
 {
     CELL3(0, d.NI, 1, d.NJ - 1, 1, d.NK - 1)
-    double S[9], G[3];
-    strain3<double>(d, d.U, d.V, d.W, d.T, i, j, k, S, G);
+    T S[9], G[3];
+    strain3<T>(d, d.U, d.V, d.W, d.T, i, j, k, S, G);
     const int c = ID3(i, j, k);
 #pragma unroll
-    for (int q = 0; q < 9; q++) d.L[q][c] = S[q];
+    for (int q = 0; q < 9; q++) sts(d, d.L[q], c, S[q]);
 #pragma unroll
-    for (int q = 0; q < 3; q++) d.DTD[q][c] = G[q];
+    for (int q = 0; q < 3; q++) sts(d, d.DTD[q], c, G[q]);
 }
 
+template <class T>
 __global__ void k3_mag(D3 d)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.n) return;
-    double s = d.L[0][c] * d.L[0][c];
+    T s = lds<T>(d, d.L[0], c) * lds<T>(d, d.L[0], c);
 #pragma unroll
-    for (int q = 1; q < 9; q++) s = s + d.L[q][c] * d.L[q][c];
-    d.MAG[c] = sqrt(2.0 * s);
+    for (int q = 1; q < 9; q++) s = s + lds<T>(d, d.L[q], c) * lds<T>(d, d.L[q], c);
+    sts(d, d.MAG, c, sqrt(scale2(s, 2.0f)));
 }
 
 // [1,2,1]^3 / 64 over the 27 neighbours of an interior cell, the reference's term
@@ -1218,6 +1291,22 @@ __global__ void k3_filter(D3 d, const double *in, double *out)
 // sum up to rounding (the terms are added in another order).
 // ---------------------------------------------------------------------------------
 __device__ __forceinline__ double *fbank(const D3 &d, int b, int q) { return d.FB + (size_t(12 * b + q)) * d.n; }
+// Bank elements hold doubles in the FP64 path and (hi, lo) pairs in the mixed path.
+template <class T>
+__device__ __forceinline__ T bank_ld(const D3 &d, int b, int q, int c);
+template <>
+__device__ __forceinline__ double bank_ld<double>(const D3 &d, int b, int q, int c) { return fbank(d, b, q)[c]; }
+template <>
+__device__ __forceinline__ dd bank_ld<dd>(const D3 &d, int b, int q, int c)
+{
+    const float2 v = reinterpret_cast<const float2 *>(fbank(d, b, q))[c];
+    return dd(v.x, v.y);
+}
+__device__ __forceinline__ void bank_st(const D3 &d, int b, int q, int c, double v) { fbank(d, b, q)[c] = v; }
+__device__ __forceinline__ void bank_st(const D3 &d, int b, int q, int c, dd v)
+{
+    reinterpret_cast<float2 *>(fbank(d, b, q))[c] = make_float2(v.hi, v.lo);
+}
 
 enum { SEP_HATS = 0, SEP_VEL = 1, SEP_HEAT = 2 };
 
@@ -1225,30 +1314,33 @@ enum { SEP_HATS = 0, SEP_VEL = 1, SEP_HEAT = 2 };
 // velocity products uu, vv, ww, uv, uw, vw and MAG*S11, S22, S33, S12, S13, S23
 // (SEP_VEL, stress_tensor_dy.f90:266-483); uT, vT, wT and MAG*dT/dx_q (SEP_HEAT,
 // stress_tensor_dy.f90:590-680).
+template <class T>
 __global__ void k3_prod(D3 d, int mode)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.n) return;
-    const double u = d.U[c], v = d.V[c], w = d.W[c], t = d.T[c], mg = d.MAG[c];
+    const T u = lds<T>(d, d.U, c), v = lds<T>(d, d.V, c), w = lds<T>(d, d.W, c), t = lds<T>(d, d.T, c);
     if (mode == SEP_HATS) {
-        fbank(d, 0, 0)[c] = u;
-        fbank(d, 0, 1)[c] = v;
-        fbank(d, 0, 2)[c] = w;
-        fbank(d, 0, 3)[c] = t;
+        bank_st(d, 0, 0, c, u);
+        bank_st(d, 0, 1, c, v);
+        bank_st(d, 0, 2, c, w);
+        bank_st(d, 0, 3, c, t);
     } else if (mode == SEP_VEL) {
-        const double uv[3] = {u, v, w};
+        const T mg = lds<T>(d, d.MAG, c);
+        const T uv[3] = {u, v, w};
 #pragma unroll
         for (int q = 0; q < 6; q++) {
             const int a = q < 3 ? q : (q == 5 ? 1 : 0), b = q < 3 ? q : (q == 3 ? 1 : 2);
-            fbank(d, 0, q)[c] = uv[a] * uv[b];
-            fbank(d, 0, 6 + q)[c] = mg * d.L[3 * a + b][c];
+            bank_st(d, 0, q, c, uv[a] * uv[b]);
+            bank_st(d, 0, 6 + q, c, mg * lds<T>(d, d.L[3 * a + b], c));
         }
     } else {
-        fbank(d, 0, 0)[c] = u * t;
-        fbank(d, 0, 1)[c] = v * t;
-        fbank(d, 0, 2)[c] = w * t;
+        const T mg = lds<T>(d, d.MAG, c);
+        bank_st(d, 0, 0, c, u * t);
+        bank_st(d, 0, 1, c, v * t);
+        bank_st(d, 0, 2, c, w * t);
 #pragma unroll
-        for (int q = 0; q < 3; q++) fbank(d, 0, 3 + q)[c] = mg * d.DTD[q][c];
+        for (int q = 0; q < 3; q++) bank_st(d, 0, 3 + q, c, mg * lds<T>(d, d.DTD[q], c));
     }
 }
 
@@ -1259,6 +1351,7 @@ struct Out4 {
 // One [1,2,1] pass over nq arrays from bank src to bank dst: dir 0 (I) for
 // i = 1..NI-1 on every (j, k); dir 1 (J) for j = 1..NJ-1 on every k; dir 2 (K) on
 // the interior, with the 1/64, into bank dst or, when out.p[0] is set, into out.p[q].
+template <class T>
 __global__ void k3_sep(D3 d, int src, int dst, int nq, int dir, Out4 out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -1267,11 +1360,10 @@ __global__ void k3_sep(D3 d, int src, int dst, int nq, int dir, Out4 out)
     if (i > d.NI - 1 || j > (dir == 0 ? d.NJ : d.NJ - 1) || k > (dir == 2 ? d.NK - 1 : d.NK)) return;
     const int c = ID3(i, j, k), o = dir == 0 ? 1 : (dir == 1 ? d.NI1 : d.NI1 * d.NJ1);
     for (int q = 0; q < nq; q++) {
-        const double *a = fbank(d, src, q);
-        const double r = (a[c - o] + 2.0 * a[c]) + a[c + o];
-        if (dir != 2) fbank(d, dst, q)[c] = r;
-        else if (out.p[0]) out.p[q][c] = r / 64.0;
-        else fbank(d, dst, q)[c] = r / 64.0;
+        const T r = (bank_ld<T>(d, src, q, c - o) + scale2(bank_ld<T>(d, src, q, c), 2.0f)) + bank_ld<T>(d, src, q, c + o);
+        if (dir != 2) bank_st(d, dst, q, c, r);
+        else if (out.p[0]) out.p[q][c] = to_d(scale2(r, 1.0f / 64.0f));
+        else bank_st(d, dst, q, c, scale2(r, 1.0f / 64.0f));
     }
 }
 
@@ -1279,25 +1371,27 @@ __global__ void k3_sep(D3 d, int src, int dst, int nq, int dir, Out4 out)
 // filtered products in bank b, accumulated into LM and MM in that order with the
 // off-diagonal ones weighted 2; the strain rate of the filtered velocity and its
 // magnitude once per cell (MAGH is kept for the heat flux).
+template <class T>
 __global__ void k3_germano(D3 d, int b)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *uh[3] = {d.UH, d.VH, d.WH};
-    double S[9], G[3];
-    strain3<double>(d, d.UH, d.VH, d.WH, nullptr, i, j, k, S, G);
-    const double magh = sqrt(2.0 * sq9<double>(S));
-    d.MAGH[c] = magh;
-    const double fw2 = d.FW[c] * d.FW[c];
-    double lm = 0.0, mm = 0.0;
+    T S[9], G[3];
+    strain3<T>(d, d.UH, d.VH, d.WH, nullptr, i, j, k, S, G);
+    const T magh = sqrt(scale2(sq9<T>(S), 2.0f));
+    d.MAGH[c] = to_d(magh);
+    const T fw2 = lds<T>(d, d.FW, c) * lds<T>(d, d.FW, c);
+    T lm, mm;
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         const int a = q < 3 ? q : (q == 5 ? 1 : 0), bb = q < 3 ? q : (q == 3 ? 1 : 2);
-        const double l = (-fbank(d, b, q)[c]) + uh[a][c] * uh[bb][c];
-        const double dout = fbank(d, b, 6 + q)[c];
-        const double fac = a == bb ? 0.5 : 0.25;
-        const double hs = S[3 * a + bb] / fac;
-        double m = ((4.0 * magh) * fac) * hs;
+        const T l = (-bank_ld<T>(d, b, q, c)) + lds<T>(d, uh[a], c) * lds<T>(d, uh[bb], c);
+        const T dout = bank_ld<T>(d, b, 6 + q, c);
+        // fac = 0.5 on the diagonal, 0.25 off it: hs = S / fac, m = ((4 magh) fac) hs
+        const float fac = a == bb ? 0.5f : 0.25f;
+        const T hs = scale2(S[3 * a + bb], 1.0f / fac);
+        T m = scale2(scale2(magh, 4.0f), fac) * hs;
         m = fw2 * (m - dout);
         if (q == 0) {
             lm = l * m;
@@ -1306,31 +1400,32 @@ __global__ void k3_germano(D3 d, int b)
             lm = lm + l * m;
             mm = mm + m * m;
         } else {
-            lm = lm + (2.0 * l) * m;
-            mm = mm + (2.0 * m) * m;
+            lm = lm + scale2(l, 2.0f) * m;
+            mm = mm + scale2(m, 2.0f) * m;
         }
     }
-    d.LM[c] = lm;
-    d.MM[c] = mm;
+    d.LM[c] = to_d(lm);
+    d.MM[c] = to_d(mm);
 }
 
 // Temperature terms P_q, R_q of the three heat-flux components from the filtered
 // products in bank b, accumulated into LM and MM.
+template <class T>
 __global__ void k3_germano_t(D3 d, int b)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *uh[3] = {d.UH, d.VH, d.WH};
     const double *M1[3] = {d.XIX, d.XIY, d.XIZ}, *M2[3] = {d.ETX, d.ETY, d.ETZ}, *M3[3] = {d.ZTX, d.ZTY, d.ZTZ};
-    const double fw2 = d.FW[c] * d.FW[c], magh = d.MAGH[c];
-    double lm = 0.0, mm = 0.0;
+    const T fw2 = lds<T>(d, d.FW, c) * lds<T>(d, d.FW, c), magh = ld<T>(d.MAGH[c]);
+    T lm, mm;
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        const double l = (-fbank(d, b, q)[c]) + uh[q][c] * d.TH[c];
-        const double dout = fbank(d, b, 3 + q)[c];
-        const double g = (dxi<double>(d, M1[q], d.TH, i, j, k) + deta<double>(d, M2[q], d.TH, i, j, k)) +
-                         dzeta<double>(d, M3[q], d.TH, i, j, k);
-        double m = ((4.0 * magh) * 0.5) * g;
+        const T l = (-bank_ld<T>(d, b, q, c)) + lds<T>(d, uh[q], c) * lds<T>(d, d.TH, c);
+        const T dout = bank_ld<T>(d, b, 3 + q, c);
+        const T g = (dxi<T>(d, M1[q], d.TH, i, j, k) + deta<T>(d, M2[q], d.TH, i, j, k)) +
+                    dzeta<T>(d, M3[q], d.TH, i, j, k);
+        T m = scale2(scale2(magh, 4.0f), 0.5f) * g;
         m = fw2 * (m - dout);
         if (q == 0) {
             lm = l * m;
@@ -1340,8 +1435,8 @@ __global__ void k3_germano_t(D3 d, int b)
             mm = mm + m * m;
         }
     }
-    d.LM[c] = lm;
-    d.MM[c] = mm;
+    d.LM[c] = to_d(lm);
+    d.MM[c] = to_d(mm);
 }
 
 // Volume-averaged coefficient over the points whose local coefficient is >= 0
@@ -1396,45 +1491,56 @@ __global__ void k3_eddy(D3 d, int slot, double *out)
         cc = d.CZ[ii + d.NI1 * jw(d, j)];
     }
     out[c] = (cc * (d.FW[c] * d.FW[c])) * d.MAG[c];
+    if (d.dfl) {
+        const dd v = fvm::dd_split(out[c]);
+        shadow(d, out)[c] = make_float2(v.hi, v.lo);
+    }
 }
 
-__device__ __forceinline__ double sgs_div(const D3 &d, const double *E, const double *const *Lc, int i, int j, int k)
+template <class T>
+__device__ __forceinline__ T sgs_div(const D3 &d, const double *E, const double *const *Lc, int i, int j, int k)
 {
     const double *M1[3] = {d.XIX, d.XIY, d.XIZ}, *M2[3] = {d.ETX, d.ETY, d.ETZ}, *M3[3] = {d.ZTX, d.ZTY, d.ZTZ};
     const int c = ID3(i, j, k), ip = ID3(i + 1, j, k), im = ID3(i - 1, j, k), jp = ID3(i, j + 1, k),
               jm = ID3(i, j - 1, k), kp = ID3(i, j, k + 1), km = ID3(i, j, k - 1);
-    double s = 0.0;
+    // 2 E at the six neighbours
+    const T ep = scale2(lds<T>(d, E, ip), 2.0f), em = scale2(lds<T>(d, E, im), 2.0f),
+            fp = scale2(lds<T>(d, E, jp), 2.0f), fm = scale2(lds<T>(d, E, jm), 2.0f),
+            gp = scale2(lds<T>(d, E, kp), 2.0f), gm = scale2(lds<T>(d, E, km), 2.0f);
+    T s;
 #pragma unroll
     for (int b = 0; b < 3; b++) {
         const double *L = Lc[b];
-        const double t1 = M1[b][c] * (-((2.0 * E[ip]) * L[ip]) + (2.0 * E[im]) * L[im]);
-        const double t2 = M2[b][c] * (-((2.0 * E[jp]) * L[jp]) + (2.0 * E[jm]) * L[jm]);
-        const double t3 = M3[b][c] * (-((2.0 * E[kp]) * L[kp]) + (2.0 * E[km]) * L[km]);
+        const T t1 = lds<T>(d, M1[b], c) * (-(ep * lds<T>(d, L, ip)) + em * lds<T>(d, L, im));
+        const T t2 = lds<T>(d, M2[b], c) * (-(fp * lds<T>(d, L, jp)) + fm * lds<T>(d, L, jm));
+        const T t3 = lds<T>(d, M3[b], c) * (-(gp * lds<T>(d, L, kp)) + gm * lds<T>(d, L, km));
         s = b == 0 ? t1 : s + t1;
         s = s + t2;
         s = s + t3;
     }
-    return 0.5 * s;
+    return scale2(s, 0.5f);
 }
 
 // SGS divergence added to the advection terms (main.f90:59-69)
+template <class T>
 __global__ void k3_sgs(D3 d)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *r0[3] = {d.L[0], d.L[1], d.L[2]}, *r1[3] = {d.L[3], d.L[4], d.L[5]}, *r2[3] = {d.L[6], d.L[7], d.L[8]};
-    const double J = d.DJAC[c];
-    d.NLX[c] = d.NLX[c] + sgs_div(d, d.EV, r0, i, j, k) * J;
-    d.NLY[c] = d.NLY[c] + sgs_div(d, d.EV, r1, i, j, k) * J;
-    d.NLZ[c] = d.NLZ[c] + sgs_div(d, d.EV, r2, i, j, k) * J;
+    const T J = lds<T>(d, d.DJAC, c);
+    d.NLX[c] = to_d(ld<T>(d.NLX[c]) + sgs_div<T>(d, d.EV, r0, i, j, k) * J);
+    d.NLY[c] = to_d(ld<T>(d.NLY[c]) + sgs_div<T>(d, d.EV, r1, i, j, k) * J);
+    d.NLZ[c] = to_d(ld<T>(d.NLZ[c]) + sgs_div<T>(d, d.EV, r2, i, j, k) * J);
 }
 
+template <class T>
 __global__ void k3_sgst(D3 d)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
     const double *g[3] = {d.DTD[0], d.DTD[1], d.DTD[2]};
-    d.ADV[c] = d.ADV[c] + sgs_div(d, d.EC, g, i, j, k) * d.DJAC[c];
+    d.ADV[c] = to_d(ld<T>(d.ADV[c]) + sgs_div<T>(d, d.EC, g, i, j, k) * lds<T>(d, d.DJAC, c));
 }
 
 // ---------------------------------------------------------------------------------
@@ -1602,6 +1708,8 @@ struct fvm3_ctx {
     // post-processing: 17 sum arrays on the device, allocated on first use
     double *post = nullptr;
     int ipost = 0, niter_pos = 0;
+    // the shadowed group's address range (arrays with (hi, lo) shadows in the mixed path)
+    double *shadow_lo = nullptr, *shadow_hi = nullptr;
 };
 
 namespace f3 {
@@ -1645,20 +1753,39 @@ void carve(Bump &b, fvm3_ctx *c)
 {
     D3 &d = c->d;
     const size_t n = c->n, jk = size_t(c->NJ + 1) * (c->NK + 1);
-    double **full[] = {&d.XG, &d.YG, &d.ZG, &d.X, &d.Y, &d.Z, &d.XIX, &d.XIY, &d.XIZ, &d.ETX, &d.ETY, &d.ETZ,
-                       &d.ZTX, &d.ZTY, &d.ZTZ, &d.DJAC, &d.Q11, &d.Q12, &d.Q13, &d.Q22, &d.Q23, &d.Q33,
-                       &d.JQ12, &d.JQ13, &d.JQ23, &d.DE,
-                       &d.DW, &d.DN, &d.DS, &d.DT, &d.DB, &d.THETA, &d.AREA1, &d.AREA2, &d.FW, &d.U, &d.V, &d.W,
-                       &d.P, &d.T, &d.U_N, &d.V_N, &d.W_N, &d.T_N, &d.NLX, &d.NLY, &d.NLZ, &d.ADV, &d.NLX_NM1,
-                       &d.NLY_NM1, &d.NLZ_NM1, &d.ADV_NM1, &d.DIFX, &d.DIFY, &d.DIFZ, &d.DIFT, &d.S_U, &d.S_V,
-                       &d.S_W, &d.U1, &d.U2, &d.U3, &d.UE, &d.UW, &d.VN, &d.VS, &d.WT, &d.WB, &d.DIVDT, &d.SU,
-                       &d.DTD[0], &d.DTD[1], &d.DTD[2], &d.MAG, &d.UH, &d.VH, &d.WH, &d.TH, &d.MAGH, &d.LM,
-                       &d.MM, &d.EV, &d.EC};
-    for (auto p : full) *p = b.take(n);
-    for (int q = 0; q < 9; q++) d.L[q] = b.take(n);
-    for (int e = 0; e < 12; e++) d.CW[e] = b.take(n);
+    // The shadowed group: the arrays the double-float kernels of the mixed path read
+    // through (hi, lo) shadows.  Taken consecutively with equal sizes, so that in the
+    // mixed path a second block taken in the same order puts every shadow at the
+    // same element offset sh from its array.
+    std::vector<double **> grp = {&d.XIX, &d.XIY, &d.XIZ, &d.ETX, &d.ETY, &d.ETZ, &d.ZTX, &d.ZTY, &d.ZTZ, &d.DJAC,
+                                  &d.FW, &d.DE, &d.DW, &d.DN, &d.DS, &d.DT, &d.DB, &d.U, &d.V, &d.W, &d.T,
+                                  &d.U_N, &d.V_N, &d.W_N, &d.T_N, &d.MAG, &d.UH, &d.VH, &d.WH, &d.TH, &d.EV, &d.EC};
+    for (int q = 0; q < 9; q++) grp.push_back(&d.L[q]);
+    for (int q = 0; q < 3; q++) grp.push_back(&d.DTD[q]);
+    for (int e = 0; e < 12; e++) grp.push_back(&d.CW[e]);
     for (int sp = 0; sp < 3; sp++)
-        for (int e = 0; e < 12; e++) d.CWA[sp][e] = b.take(n);
+        for (int e = 0; e < 12; e++) grp.push_back(&d.CWA[sp][e]);
+    for (auto p : grp) *p = b.take(n);
+    d.dfl = c->p.precision == FVM_MIXED ? 1 : 0;
+    d.sh = 0;
+    if (d.dfl) {
+        double *first = nullptr;
+        for (size_t q = 0; q < grp.size(); q++) {
+            double *t = b.take(n);
+            if (q == 0) first = t;
+        }
+        d.sh = b.base ? (long long)(first - d.XIX) : 0;
+    }
+    if (b.base) {
+        c->shadow_lo = d.XIX;
+        c->shadow_hi = *grp.back() + n;
+    }
+    double **full[] = {&d.XG, &d.YG, &d.ZG, &d.X, &d.Y, &d.Z, &d.Q11, &d.Q12, &d.Q13, &d.Q22, &d.Q23, &d.Q33,
+                       &d.JQ12, &d.JQ13, &d.JQ23, &d.THETA, &d.AREA1, &d.AREA2, &d.P, &d.NLX, &d.NLY, &d.NLZ,
+                       &d.ADV, &d.NLX_NM1, &d.NLY_NM1, &d.NLZ_NM1, &d.ADV_NM1, &d.DIFX, &d.DIFY, &d.DIFZ, &d.DIFT,
+                       &d.S_U, &d.S_V, &d.S_W, &d.U1, &d.U2, &d.U3, &d.UE, &d.UW, &d.VN, &d.VS, &d.WT, &d.WB,
+                       &d.DIVDT, &d.SU, &d.MAGH, &d.LM, &d.MM};
+    for (auto p : full) *p = b.take(n);
     for (int q = 0; q < 9; q++) d.MD[q] = d.L[q];   // metric derivatives live in the strain arrays at setup
     double **perjk[] = {&d.FFU, &d.FFV, &d.FFW, &d.FFT};
     for (auto p : perjk) *p = b.take(jk);
@@ -1730,6 +1857,49 @@ int halo(fvm3_ctx *c, std::initializer_list<double *> arrs)
     k3_halo_k<<<dim3((c->NI + 1 + 127) / 128, c->NJ + 1), 128, 0, c->stream>>>(c->d, A);
     F3CHECK(c);
     return FVM_OK;
+}
+
+// Periodic copy of the shadows of shadowed arrays (mixed path).
+int halo_shadows(fvm3_ctx *c, const std::vector<double *> &arrs)
+{
+    if (!c->d.dfl) return FVM_OK;
+    Arrs A{};
+    A.n = 0;
+    for (double *a : arrs) A.a[A.n++] = a + c->d.sh;
+    k3_halo_j<<<dim3((c->NI + 1 + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(c->d, A);
+    k3_halo_k<<<dim3((c->NI + 1 + 127) / 128, c->NJ + 1), 128, 0, c->stream>>>(c->d, A);
+    F3CHECK(c);
+    return FVM_OK;
+}
+
+// Refresh the shadows of shadowed arrays from their doubles (mixed path; a no-op
+// in the FP64 path).
+int refresh(fvm3_ctx *c, const std::vector<double *> &arrs)
+{
+    if (!c->d.dfl) return FVM_OK;
+    Arrs A{};
+    A.n = 0;
+    for (size_t q = 0; q < arrs.size(); q++) {
+        A.a[A.n++] = arrs[q];
+        if (A.n == 16 || q + 1 == arrs.size()) {
+            k3_shadow<<<(c->n + 255) / 256, 256, 0, c->stream>>>(c->d, A);
+            A.n = 0;
+        }
+    }
+    F3CHECK(c);
+    return FVM_OK;
+}
+
+// The geometry-only arrays of the shadowed group, after the setup.
+int refresh_constants(fvm3_ctx *c)
+{
+    D3 &d = c->d;
+    std::vector<double *> a = {d.XIX, d.XIY, d.XIZ, d.ETX, d.ETY, d.ETZ, d.ZTX, d.ZTY, d.ZTZ, d.DJAC, d.FW,
+                               d.DE, d.DW, d.DN, d.DS, d.DT, d.DB};
+    for (int e = 0; e < 12; e++) a.push_back(d.CW[e]);
+    for (int sp = 0; sp < 3; sp++)
+        for (int e = 0; e < 12; e++) a.push_back(d.CWA[sp][e]);
+    return refresh(c, a);
 }
 
 int line(fvm3_ctx *c, int set, const double *SU, double *phi, int colour, const PCtl *stop = nullptr)
@@ -1804,6 +1974,7 @@ int setup_grid(fvm3_ctx *c)
         k3_factor<<<(d.sys[s].lines + 63) / 64, 64, 0, st>>>(d, d.cf[s], d.sys[s], fam, fam != 0);
     }
     F3CHECK(c);
+    F3RC(refresh_constants(c));
     // sum of the wall areas in the reference's loop order (init.f90:186-190)
     std::vector<double> a1(c->n), a2(c->n), dj(c->n);
     F3CUDA(c, cudaMemcpyAsync(a1.data(), d.AREA1, sizeof(double) * c->n, cudaMemcpyDeviceToHost, st));
@@ -1826,6 +1997,15 @@ int setup_grid(fvm3_ctx *c)
     return FVM_OK;
 }
 
+// The stencils of the SGS model, DIF, NL, P_SOURCE and the AF right-hand sides run
+// in double-float in the mixed path (FP64 in memory) and in FP64 otherwise.
+static inline bool dfloat(const fvm3_ctx *c) { return c->p.precision == FVM_MIXED; }
+#define F3_LAUNCH(c, K, grid, block, ...)                                         \
+    do {                                                                          \
+        if (dfloat(c)) K<dd><<<(grid), (block), 0, (c)->stream>>>(__VA_ARGS__);   \
+        else K<double><<<(grid), (block), 0, (c)->stream>>>(__VA_ARGS__);         \
+    } while (0)
+
 // One predictor sweep set (three AF sweeps) of a field: kind 0 U, 1 V or W, 2 T.
 int predictor(fvm3_ctx *c, int kind, double *phi, const double *phin, const double *ina, const double *inb,
               const double *inc, const double *ind, const double *ff)
@@ -1833,8 +2013,9 @@ int predictor(fvm3_ctx *c, int kind, double *phi, const double *phin, const doub
     D3 &d = c->d;
     const int base = kind == 2 ? 3 : 0;
     for (int split = 0; split < 3; split++) {
-        k3_af_rhs<double><<<g_int(c), B_INT, 0, c->stream>>>(d, d.cf[base + split], split, kind, phi, phin, ina, inb,
-                                                             inc, ind, ff);
+        F3RC(refresh(c, {phi}));
+        F3_LAUNCH(c, k3_af_rhs, g_int(c), B_INT, d, d.cf[base + split], split, kind, phi, phin, ina, inb, inc, ind,
+                  ff);
         k3_ghost<<<dim3((c->NJ + 1 + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, phi, ff, kind);
         F3RC(halo(c, {phi}));
         F3RC(line(c, base + split, d.SU, phi, 0));
@@ -1924,10 +2105,11 @@ int sep_filter(fvm3_ctx *c, int mode)
     const int nq = mode == SEP_HATS ? 4 : (mode == SEP_VEL ? 12 : 6);
     Out4 none{}, hats{};
     if (mode == SEP_HATS) hats = Out4{{d.UH, d.VH, d.WH, d.TH}};
-    k3_prod<<<g_lin(c), 256, 0, c->stream>>>(d, mode);
-    k3_sep<<<dim3((c->NI - 1 + 31) / 32, (c->NJ + 1 + 3) / 4, c->NK + 1), B_INT, 0, c->stream>>>(d, 0, 1, nq, 0, none);
-    k3_sep<<<dim3((c->NI - 1 + 31) / 32, (c->NJ - 1 + 3) / 4, c->NK + 1), B_INT, 0, c->stream>>>(d, 1, 0, nq, 1, none);
-    k3_sep<<<g_int(c), B_INT, 0, c->stream>>>(d, 0, 1, nq, 2, mode == SEP_HATS ? hats : none);
+    F3_LAUNCH(c, k3_prod, g_lin(c), 256, d, mode);
+    const dim3 gi((c->NI - 1 + 31) / 32, (c->NJ + 1 + 3) / 4, c->NK + 1), gj((c->NI - 1 + 31) / 32, (c->NJ - 1 + 3) / 4, c->NK + 1);
+    F3_LAUNCH(c, k3_sep, gi, B_INT, d, 0, 1, nq, 0, none);
+    F3_LAUNCH(c, k3_sep, gj, B_INT, d, 1, 0, nq, 1, none);
+    F3_LAUNCH(c, k3_sep, g_int(c), B_INT, d, 0, 1, nq, 2, mode == SEP_HATS ? hats : none);
     F3CHECK(c);
     return FVM_OK;
 }
@@ -1936,28 +2118,33 @@ int sgs(fvm3_ctx *c)
 {
     D3 &d = c->d;
     cudaStream_t st = c->stream;
-    k3_strain<<<dim3((c->NI + 1 + 31) / 32, (c->NJ - 1 + 3) / 4, c->NK - 1), B_INT, 0, st>>>(d);
+    const dim3 gs((c->NI + 1 + 31) / 32, (c->NJ - 1 + 3) / 4, c->NK - 1);
+    F3RC(refresh(c, {d.U, d.V, d.W, d.T}));
+    F3_LAUNCH(c, k3_strain, gs, B_INT, d);   // L and DTD with their shadows
     F3RC(halo(c, {d.L[0], d.L[1], d.L[2], d.L[3], d.L[4], d.L[5], d.L[6], d.L[7], d.L[8], d.DTD[0], d.DTD[1],
                   d.DTD[2]}));
-    k3_mag<<<g_lin(c), 256, 0, st>>>(d);
+    F3RC(halo_shadows(c, {d.L[0], d.L[1], d.L[2], d.L[3], d.L[4], d.L[5], d.L[6], d.L[7], d.L[8], d.DTD[0],
+                          d.DTD[1], d.DTD[2]}));
+    F3_LAUNCH(c, k3_mag, g_lin(c), 256, d);
     F3RC(sep_filter(c, SEP_HATS));
     F3RC(bcu(c, d.UH, d.FFU, 0));
     F3RC(bcu(c, d.VH, d.FFV, 1));
     F3RC(bcu(c, d.WH, d.FFW, 1));
     F3RC(bcu(c, d.TH, d.FFT, 2));
+    F3RC(refresh(c, {d.UH, d.VH, d.WH, d.TH}));
     F3RC(sep_filter(c, SEP_VEL));
-    k3_germano<<<g_int(c), B_INT, 0, st>>>(d, 1);
+    F3_LAUNCH(c, k3_germano, g_int(c), B_INT, d, 1);
     if (d.les_zavg) k3_czavg<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1), 128, 0, st>>>(d);
     else k3_cvol<<<d.nblk, 256, 0, st>>>(d, 0);
     k3_eddy<<<g_lin(c), 256, 0, st>>>(d, 0, d.EV);
-    k3_sgs<<<g_int(c), B_INT, 0, st>>>(d);
+    F3_LAUNCH(c, k3_sgs, g_int(c), B_INT, d);
     if (d.thermal) {
         F3RC(sep_filter(c, SEP_HEAT));
-        k3_germano_t<<<g_int(c), B_INT, 0, st>>>(d, 1);
+        F3_LAUNCH(c, k3_germano_t, g_int(c), B_INT, d, 1);
         if (d.les_zavg) k3_czavg<<<dim3((c->NI - 1 + 127) / 128, c->NJ - 1), 128, 0, st>>>(d);
         else k3_cvol<<<d.nblk, 256, 0, st>>>(d, 1);
         k3_eddy<<<g_lin(c), 256, 0, st>>>(d, 1, d.EC);
-        k3_sgst<<<g_int(c), B_INT, 0, st>>>(d);
+        F3_LAUNCH(c, k3_sgst, g_int(c), B_INT, d);
     }
     F3CHECK(c);
     return FVM_OK;
@@ -1990,7 +2177,7 @@ int begin_step(fvm3_ctx *c)   // main.f90:37-44, the far-field values of BCU/BCT
     k3_begin<<<g_lin(c), 256, 0, c->stream>>>(d);
     k3_farfield<<<dim3((c->NJ + 127) / 128, c->NK - 1), 128, 0, c->stream>>>(d);
     F3CHECK(c);
-    return FVM_OK;
+    return refresh(c, {d.U_N, d.V_N, d.W_N, d.T_N});
 }
 
 int contra_vel(fvm3_ctx *c, int with_div)   // CONTRA_VEL; with_div: the Poisson source too
@@ -2005,21 +2192,21 @@ int contra_vel(fvm3_ctx *c, int with_div)   // CONTRA_VEL; with_div: the Poisson
 
 int nl_all(fvm3_ctx *c)   // main.f90:50-57
 {
-    k3_explicit<<<g_int(c), B_INT, 0, c->stream>>>(c->d, c->d.thermal);
+    F3_LAUNCH(c, k3_explicit, g_int(c), B_INT, c->d, c->d.thermal);
     F3CHECK(c);
     return FVM_OK;
 }
 
 int dif_all(fvm3_ctx *c)   // main.f90:72-75
 {
-    k3_dif<double><<<g_int(c), B_INT, 0, c->stream>>>(c->d, c->d.thermal);
+    F3_LAUNCH(c, k3_dif, g_int(c), B_INT, c->d, c->d.thermal);
     F3CHECK(c);
     return FVM_OK;
 }
 
 int p_source(fvm3_ctx *c)   // P_SOURCE(P)
 {
-    k3_psource<<<g_int(c), B_INT, 0, c->stream>>>(c->d);
+    F3_LAUNCH(c, k3_psource, g_int(c), B_INT, c->d);
     F3CHECK(c);
     return FVM_OK;
 }
@@ -2061,7 +2248,7 @@ int iter_p(fvm3_ctx *c)   // main.f90:99-104: CONTRA_VEL, ITER_P, BCP
 int correct(fvm3_ctx *c)   // main.f90:106-140: P_SOURCE, u += dt S/J, reference pressure, BCU
 {
     D3 &d = c->d;
-    k3_psource<<<g_int(c), B_INT, 0, c->stream>>>(d);
+    F3_LAUNCH(c, k3_psource, g_int(c), B_INT, d);
     k3_grad<<<g_int(c), B_INT, 0, c->stream>>>(d, +1.0);
     k3_pref<<<1, 32, 0, c->stream>>>(d);
     k3_pshift<<<g_lin(c), 256, 0, c->stream>>>(d);
@@ -2182,6 +2369,8 @@ int fvm3_create(const fvm3_params *p, fvm3_ctx **out)
     f3::D3 &d = c->d;
     d.NI = p->ni; d.NJ = p->nj; d.NK = p->nk; d.NI1 = p->ni + 1; d.NJ1 = p->nj + 1; d.n = c->n;
     d.re = p->re; d.pe = p->re * p->pr; d.dt = p->dt; d.rdt = 1.0 / p->dt; d.tin = p->tin; d.t_wall = p->t_wall;
+    d.r2re_dt = (2.0 * d.re) / d.dt;
+    d.r2pe_dt = (2.0 * d.pe) / d.dt;
     d.pi = 4.0 * std::atan(1.0); d.resimax = p->resimax; d.ref_a = p->ref_a;
     d.res_every = p->res_every < 1 ? 1 : p->res_every;
     d.nswpp = ((p->nswpp + d.res_every - 1) / d.res_every) * d.res_every;
@@ -2295,6 +2484,7 @@ int fvm3_set_array(fvm3_ctx *c, const char *name, const double *in)
     double *a = f3::array_by_name(c, name);
     if (!a) return f3::bad3(c, "unknown array name");
     F3CUDA(c, cudaMemcpyAsync(a, in, sizeof(double) * c->n, cudaMemcpyHostToDevice, c->stream));
+    if (c->d.dfl && a >= c->shadow_lo && a < c->shadow_hi) F3RC(f3::refresh(c, {a}));
     F3CUDA(c, cudaStreamSynchronize(c->stream));
     c->init_done = true;
     return FVM_OK;
@@ -2308,6 +2498,7 @@ int fvm3_sgs(fvm3_ctx *c, fvm3_coeffs *out)
     f3::D3 &d = c->d;
     f3::k3_begin<<<f3::g_lin(c), 256, 0, c->stream>>>(d);
     f3::k3_farfield<<<dim3((c->NJ + 127) / 128, c->NK - 1), 128, 0, c->stream>>>(d);
+    F3RC(f3::refresh(c, {d.U_N, d.V_N, d.W_N, d.T_N}));
     F3CUDA(c, cudaMemsetAsync(d.NLX, 0, sizeof(double) * c->n, c->stream));
     F3CUDA(c, cudaMemsetAsync(d.NLY, 0, sizeof(double) * c->n, c->stream));
     F3CUDA(c, cudaMemsetAsync(d.NLZ, 0, sizeof(double) * c->n, c->stream));
