@@ -14,6 +14,7 @@
 // Line solves reuse the group solver of the 2-D path (precomputed LU factors in
 // chunk-interleaved layout, warp scans of affine maps, Sherman-Morrison for the
 // cyclic lines).
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -24,6 +25,20 @@
 #include "fvm_df.cuh"
 #include "fvm_internal.cuh"
 #include "../../include/fvm3d.h"
+
+namespace fvm {
+// warp shuffles of a double-float value (the group line solver's scans)
+template <>
+__device__ __forceinline__ dd shfl_up<dd>(dd v, int s)
+{
+    return dd(__shfl_up_sync(0xffffffffu, v.hi, s), __shfl_up_sync(0xffffffffu, v.lo, s));
+}
+template <>
+__device__ __forceinline__ dd shfl_down<dd>(dd v, int s)
+{
+    return dd(__shfl_down_sync(0xffffffffu, v.hi, s), __shfl_down_sync(0xffffffffu, v.lo, s));
+}
+}  // namespace fvm
 
 namespace f3 {
 
@@ -40,6 +55,11 @@ using fvm::WARP;
 struct Coef3 {
     double *AP, *AE, *AW, *AN, *AS, *AT, *AB;
     double *awall, *afar;   // (NJ+1)*(NK+1)
+};
+
+// Double-float copies of a predictor set's line factors (mixed path).
+struct LineDD {
+    dd *invD, *fa, *fb, *z, *cv, *sinv;
 };
 
 struct D3 {
@@ -72,6 +92,7 @@ struct D3 {
     // coefficient sets: [0..2] velocity splits, [3..5] temperature splits, [6] Poisson
     Coef3 cf[7];
     LineSys sys[7];
+    LineDD sysd[6];   // mixed path: the factors of the six predictor sets as (hi, lo) pairs
     // MIXED Poisson: FP32 residual and correction, FP32 copies of the transverse
     // couplings of the Poisson set
     float *RF, *DF, *ANf, *ASf, *ATf, *ABf;
@@ -125,32 +146,35 @@ __device__ __forceinline__ void sts(const D3 &d, double *p, int c, dd v)
 
 // ---------------------------------------------------------------------------------
 // Periodic copy of MPI_X (mpi_x.f90:25-51): J planes for every K, then K planes for
-// every J (two launches).  Up to 16 arrays per launch.
+// every J, as one launch (k3_halo).  Up to 16 arrays per launch.
 // ---------------------------------------------------------------------------------
 struct Arrs {
     double *a[16];
     int n;
 };
 
-__global__ void k3_halo_j(D3 d, Arrs A)
+// Both copies in one launch: the final value of every ghost (j in {0, NJ} or k in
+// {0, NK}) is the interior value at the wrapped indices, which the J-then-K pair
+// produces; grid y < NK+1 takes the J ghosts of plane k = y, the rest the K ghosts
+// of row j = y - NK - 1 (the corner ghosts are written twice with the same value).
+__global__ void k3_halo(D3 d, Arrs A)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
-    if (i > d.NI || k > d.NK) return;
-    for (int q = 0; q < A.n; q++) {
-        double *a = A.a[q];
-        a[ID3(i, 0, k)] = a[ID3(i, d.NJ - 1, k)];
-        a[ID3(i, d.NJ, k)] = a[ID3(i, 1, k)];
-    }
-}
-
-__global__ void k3_halo_k(D3 d, Arrs A)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i > d.NI || j > d.NJ) return;
-    for (int q = 0; q < A.n; q++) {
-        double *a = A.a[q];
-        a[ID3(i, j, 0)] = a[ID3(i, j, d.NK - 1)];
-        a[ID3(i, j, d.NK)] = a[ID3(i, j, 1)];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+    if (i > d.NI) return;
+    if (r <= d.NK) {
+        const int k = r, ks = kw(d, k);
+        for (int q = 0; q < A.n; q++) {
+            double *a = A.a[q];
+            a[ID3(i, 0, k)] = a[ID3(i, d.NJ - 1, ks)];
+            a[ID3(i, d.NJ, k)] = a[ID3(i, 1, ks)];
+        }
+    } else {
+        const int j = r - d.NK - 1, js = jw(d, j);
+        for (int q = 0; q < A.n; q++) {
+            double *a = A.a[q];
+            a[ID3(i, j, 0)] = a[ID3(i, js, d.NK - 1)];
+            a[ID3(i, j, d.NK)] = a[ID3(i, js, 1)];
+        }
     }
 }
 
@@ -633,13 +657,16 @@ __device__ __forceinline__ void couple_coefs(const Coef3 &cf, const double *&c1,
     c4 = FAM == 2 ? cf.AS : cf.AB;
 }
 
-template <int M, int NW, int FAM>
+// T: double (FP64 path, every set) or dd (mixed path, the predictor sets 0..5, whose
+// couplings and phi are read through their shadows and factors from sd; phi is
+// stored with its shadow, so the second colour reads the first colour's values).
+template <int M, int NW, int FAM, class T = double>
 __global__ void __launch_bounds__(128) k3_line(D3 d, LineSys s, Coef3 cf, const double *SU, double *phi, int colour,
-                                               const PCtl *stop)
+                                               const PCtl *stop, LineDD sd)
 {
     constexpr int TG = WARP * NW, G = 4 / NW;
-    __shared__ double sm[G][TG * M + M * NW + 1];
-    __shared__ double xch[G][2 * NW];
+    __shared__ T sm[G][TG * M + M * NW + 1];
+    __shared__ T xch[G][2 * NW];
     if (stop && stop->done) return;   // the Poisson loop has ended
     int gl, t, gib;
     fvm::group_of<NW>(gl, t, gib);
@@ -650,27 +677,55 @@ __global__ void __launch_bounds__(128) k3_line(D3 d, LineSys s, Coef3 cf, const 
     const LineGeo g = line_geo<FAM>(d, L);
     const double *c1, *c2, *c3, *c4;
     couple_coefs<FAM>(cf, c1, c2, c3, c4);
-    double v[M];
+    T v[M];
 #pragma unroll
     for (int q = 0; q < M; q++) {
         const int e = q * TG + t;
-        v[q] = 0.0;
+        v[q] = T(0);
         if (active && e < n) {
             const int c = g.base + e * g.stride;
             // the four transverse couplings and the source as fused multiply-adds
-            v[q] = fma(c1[c], phi[c + g.o1], fma(c2[c], phi[c + g.o2], fma(c3[c], phi[c + g.o3],
-                                                                             fma(c4[c], phi[c + g.o4], SU[c]))));
+            v[q] = fma(lds<T>(d, c1, c), lds<T>(d, phi, c + g.o1),
+                       fma(lds<T>(d, c2, c), lds<T>(d, phi, c + g.o2),
+                           fma(lds<T>(d, c3, c), lds<T>(d, phi, c + g.o3),
+                               fma(lds<T>(d, c4, c), lds<T>(d, phi, c + g.o4), ld<T>(SU[c])))));
         }
     }
-    fvm::to_chunks<double, M, NW>(v, sm[gib], t);
+    fvm::to_chunks<T, M, NW>(v, sm[gib], t);
     const size_t base = size_t(L) * TG * M;
-    fvm::group_apply<double, M, NW>(v, s.invD + base, s.fa + base, s.fb + base, t, xch[gib]);
-    if (FAM != 0) fvm::group_cyclic_fix<double, M, NW>(v, s.z + base, s.cv[L], s.sinv[L], n, t, xch[gib]);
-    fvm::to_interleaved<double, M, NW>(v, sm[gib], t);
+    if constexpr (std::is_same<T, double>::value) {
+        fvm::group_apply<double, M, NW>(v, s.invD + base, s.fa + base, s.fb + base, t, xch[gib]);
+        if (FAM != 0) fvm::group_cyclic_fix<double, M, NW>(v, s.z + base, s.cv[L], s.sinv[L], n, t, xch[gib]);
+    } else {
+        fvm::group_apply<dd, M, NW>(v, sd.invD + base, sd.fa + base, sd.fb + base, t, xch[gib]);
+        if (FAM != 0) fvm::group_cyclic_fix<dd, M, NW>(v, sd.z + base, sd.cv[L], sd.sinv[L], n, t, xch[gib]);
+    }
+    fvm::to_interleaved<T, M, NW>(v, sm[gib], t);
 #pragma unroll
     for (int q = 0; q < M; q++) {
         const int e = q * TG + t;
-        if (active && e < n) phi[g.base + e * g.stride] = v[q];
+        if (active && e < n) sts(d, phi, g.base + e * g.stride, v[q]);
+    }
+}
+
+// The (hi, lo) pairs nearest to a predictor set's FP64 line factors (mixed path).
+__device__ __forceinline__ dd dd_near(double x)
+{
+    const float h = (float)x;
+    return dd(h, (float)(x - (double)h));
+}
+__global__ void k3_factor_dd(LineSys s, LineDD sd, size_t cnt)
+{
+    const size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (q < cnt) {
+        sd.invD[q] = dd_near(s.invD[q]);
+        sd.fa[q] = dd_near(s.fa[q]);
+        sd.fb[q] = dd_near(s.fb[q]);
+        if (s.cyclic) sd.z[q] = dd_near(s.z[q]);
+    }
+    if (s.cyclic && q < (size_t)s.lines) {
+        sd.cv[q] = dd_near(s.cv[q]);
+        sd.sinv[q] = dd_near(s.sinv[q]);
     }
 }
 
@@ -905,11 +960,28 @@ __global__ void k3_af_rhs(D3 d, Coef3 cf, int split, int kind, const double *phi
     d.SU[c] = to_d(su);
 }
 
-// u += sign * dt * S / J (main.f90:84-86, 104-106)
+// u += sign * dt * S / J (main.f90:84-86, 104-106).  The update of the state is
+// FP64 in both paths; the mixed path forms the increments dt S / J in double-float.
+template <class T>
 __global__ void k3_grad(D3 d, double sign)
 {
     CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
     const int c = ID3(i, j, k);
+    if constexpr (!std::is_same<T, double>::value) {
+        const T rj = T(1) / lds<T>(d, d.DJAC, c), f = ld<T>(d.dt);
+        const double iu = to_d((f * ld<T>(d.S_U[c])) * rj), iv = to_d((f * ld<T>(d.S_V[c])) * rj),
+                     iw = to_d((f * ld<T>(d.S_W[c])) * rj);
+        if (sign < 0) {
+            d.U[c] = d.U[c] - iu;
+            d.V[c] = d.V[c] - iv;
+            d.W[c] = d.W[c] - iw;
+        } else {
+            d.U[c] = d.U[c] + iu;
+            d.V[c] = d.V[c] + iv;
+            d.W[c] = d.W[c] + iw;
+        }
+        return;
+    }
     const double f = d.dt;
     if (sign < 0) {
         d.U[c] = d.U[c] - (f * d.S_U[c]) / d.DJAC[c];
@@ -1439,6 +1511,23 @@ __global__ void k3_germano_t(D3 d, int b)
     d.MM[c] = to_d(mm);
 }
 
+// (0.5 lm) / mm >= 0, decided without the division (one FP64 division costs several
+// FP64-pipe instructions on GB300) and exactly as the quotient would decide it,
+// including zero, infinite and NaN operands and a negative quotient that underflows
+// to -0 (|q| <= 2^-1075).
+__device__ __forceinline__ bool coef_nonneg(double lm, double mm)
+{
+    const double h = 0.5 * lm;
+    if (h != h || mm != mm) return false;
+    const double ah = fabs(h), am = fabs(mm);
+    const bool same = signbit(h) == signbit(mm);
+    if (am == 0.0) return h != 0.0 && same;                     // +-inf or NaN
+    if (am > DBL_MAX) return ah <= DBL_MAX;                     // finite / inf = +-0
+    if (ah > DBL_MAX) return same;                              // inf / finite
+    if (same) return true;                                      // positive or +-0
+    return (ah * 0x1p600) * 0x1p475 <= am;                      // rounds to -0
+}
+
 // Volume-averaged coefficient over the points whose local coefficient is >= 0
 // (stress_tensor_dy.f90:486-517): result in scal[slot].
 __global__ void __launch_bounds__(256) k3_cvol(D3 d, int slot)
@@ -1449,8 +1538,7 @@ __global__ void __launch_bounds__(256) k3_cvol(D3 d, int slot)
     double lm = 0.0, mm = 0.0, inc = 0.0;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         const int i = e % ni1 + 1, j = (e / ni1) % nj1 + 1, k = e / (ni1 * nj1) + 1, c = ID3(i, j, k);
-        const double cs = (0.5 * d.LM[c]) / d.MM[c];
-        if (cs >= 0.0) {
+        if (coef_nonneg(d.LM[c], d.MM[c])) {
             lm += d.LM[c];
             mm += d.MM[c];
             inc += 1.0;
@@ -1765,6 +1853,10 @@ void carve(Bump &b, fvm3_ctx *c)
     for (int e = 0; e < 12; e++) grp.push_back(&d.CW[e]);
     for (int sp = 0; sp < 3; sp++)
         for (int e = 0; e < 12; e++) grp.push_back(&d.CWA[sp][e]);
+    for (int st = 0; st < 6; st++) {   // the couplings of the predictor sets
+        Coef3 &cf = d.cf[st];
+        for (double **p : {&cf.AE, &cf.AW, &cf.AN, &cf.AS, &cf.AT, &cf.AB}) grp.push_back(p);
+    }
     for (auto p : grp) *p = b.take(n);
     d.dfl = c->p.precision == FVM_MIXED ? 1 : 0;
     d.sh = 0;
@@ -1792,8 +1884,9 @@ void carve(Bump &b, fvm3_ctx *c)
     d.CZ = b.take(size_t(c->NI + 1) * (c->NJ + 1));
     for (int s = 0; s < 7; s++) {
         Coef3 &cf = d.cf[s];
-        double **arr[] = {&cf.AP, &cf.AE, &cf.AW, &cf.AN, &cf.AS, &cf.AT, &cf.AB};
-        for (auto p : arr) *p = b.take(n);
+        cf.AP = b.take(n);
+        if (s == 6)
+            for (double **p : {&cf.AE, &cf.AW, &cf.AN, &cf.AS, &cf.AT, &cf.AB}) *p = b.take(n);
         cf.awall = b.take(jk);
         cf.afar = b.take(jk);
     }
@@ -1830,6 +1923,15 @@ void carve(Bump &b, fvm3_ctx *c)
             ls.cvf = reinterpret_cast<float *>(b.take(F.lines));
             ls.sinvf = reinterpret_cast<float *>(b.take(F.lines));
         }
+        if (s < 6 && d.dfl) {
+            LineDD &sd = d.sysd[s];
+            sd.invD = reinterpret_cast<dd *>(b.take(cnt));
+            sd.fa = reinterpret_cast<dd *>(b.take(cnt));
+            sd.fb = reinterpret_cast<dd *>(b.take(cnt));
+            sd.z = ls.cyclic ? reinterpret_cast<dd *>(b.take(cnt)) : nullptr;
+            sd.cv = ls.cyclic ? reinterpret_cast<dd *>(b.take(F.lines)) : nullptr;
+            sd.sinv = ls.cyclic ? reinterpret_cast<dd *>(b.take(F.lines)) : nullptr;
+        }
     }
     float **f32[] = {&d.RF, &d.DF, &d.ANf, &d.ASf, &d.ATf, &d.ABf};
     for (auto p : f32) *p = reinterpret_cast<float *>(b.take((n + 1) / 2));
@@ -1853,8 +1955,7 @@ int halo(fvm3_ctx *c, std::initializer_list<double *> arrs)
     Arrs A{};
     A.n = 0;
     for (double *a : arrs) A.a[A.n++] = a;
-    k3_halo_j<<<dim3((c->NI + 1 + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(c->d, A);
-    k3_halo_k<<<dim3((c->NI + 1 + 127) / 128, c->NJ + 1), 128, 0, c->stream>>>(c->d, A);
+    k3_halo<<<dim3((c->NI + 1 + 127) / 128, c->NK + 1 + c->NJ + 1), 128, 0, c->stream>>>(c->d, A);
     F3CHECK(c);
     return FVM_OK;
 }
@@ -1866,8 +1967,7 @@ int halo_shadows(fvm3_ctx *c, const std::vector<double *> &arrs)
     Arrs A{};
     A.n = 0;
     for (double *a : arrs) A.a[A.n++] = a + c->d.sh;
-    k3_halo_j<<<dim3((c->NI + 1 + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(c->d, A);
-    k3_halo_k<<<dim3((c->NI + 1 + 127) / 128, c->NJ + 1), 128, 0, c->stream>>>(c->d, A);
+    k3_halo<<<dim3((c->NI + 1 + 127) / 128, c->NK + 1 + c->NJ + 1), 128, 0, c->stream>>>(c->d, A);
     F3CHECK(c);
     return FVM_OK;
 }
@@ -1899,6 +1999,8 @@ int refresh_constants(fvm3_ctx *c)
     for (int e = 0; e < 12; e++) a.push_back(d.CW[e]);
     for (int sp = 0; sp < 3; sp++)
         for (int e = 0; e < 12; e++) a.push_back(d.CWA[sp][e]);
+    for (int st = 0; st < 6; st++)
+        for (double *p : {d.cf[st].AE, d.cf[st].AW, d.cf[st].AN, d.cf[st].AS, d.cf[st].AT, d.cf[st].AB}) a.push_back(p);
     return refresh(c, a);
 }
 
@@ -1914,9 +2016,19 @@ int line(fvm3_ctx *c, int set, const double *SU, double *phi, int colour, const 
     const int blocks = fvm::line_blocks(per, s.NW);
     bool ok = fvm::dispatch_line(s, [&](auto m, auto nw) {
         constexpr int M = decltype(m)::value, NW = decltype(nw)::value;
-        if (fam == 0) k3_line<M, NW, 0><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop);
-        else if (fam == 1) k3_line<M, NW, 1><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop);
-        else k3_line<M, NW, 2><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop);
+        const LineDD none{};
+        if (d.dfl && set < 6) {   // predictor sets of the mixed path: double-float
+            const LineDD &sd = d.sysd[set];
+            if (fam == 0) k3_line<M, NW, 0, dd><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop, sd);
+            else if (fam == 1) k3_line<M, NW, 1, dd><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop, sd);
+            else k3_line<M, NW, 2, dd><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop, sd);
+        } else if (fam == 0) {
+            k3_line<M, NW, 0><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop, none);
+        } else if (fam == 1) {
+            k3_line<M, NW, 1><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop, none);
+        } else {
+            k3_line<M, NW, 2><<<blocks, 128, 0, c->stream>>>(d, s, d.cf[set], SU, phi, colour, stop, none);
+        }
     });
     if (!ok) {
         c->err = "line length above 512 cells is not supported";
@@ -1973,6 +2085,12 @@ int setup_grid(fvm3_ctx *c)
         const int fam = s == 6 ? 0 : s % 3;
         k3_factor<<<(d.sys[s].lines + 63) / 64, 64, 0, st>>>(d, d.cf[s], d.sys[s], fam, fam != 0);
     }
+    if (d.dfl)
+        for (int s = 0; s < 6; s++) {
+            const LineSys &ls = d.sys[s];
+            const size_t cnt = size_t(ls.lines) * WARP * ls.NW * ls.M;
+            k3_factor_dd<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(ls, d.sysd[s], cnt);
+        }
     F3CHECK(c);
     F3RC(refresh_constants(c));
     // sum of the wall areas in the reference's loop order (init.f90:186-190)
@@ -2230,7 +2348,7 @@ int bcu_all(fvm3_ctx *c)   // BCU of U, V, W
 
 int remove_grad(fvm3_ctx *c)   // main.f90:90-97: u -= dt S/J, BCU
 {
-    k3_grad<<<g_int(c), B_INT, 0, c->stream>>>(c->d, -1.0);
+    F3_LAUNCH(c, k3_grad, g_int(c), B_INT, c->d, -1.0);
     F3CHECK(c);
     return bcu_all(c);
 }
@@ -2249,7 +2367,7 @@ int correct(fvm3_ctx *c)   // main.f90:106-140: P_SOURCE, u += dt S/J, reference
 {
     D3 &d = c->d;
     F3_LAUNCH(c, k3_psource, g_int(c), B_INT, d);
-    k3_grad<<<g_int(c), B_INT, 0, c->stream>>>(d, +1.0);
+    F3_LAUNCH(c, k3_grad, g_int(c), B_INT, d, +1.0);
     k3_pref<<<1, 32, 0, c->stream>>>(d);
     k3_pshift<<<g_lin(c), 256, 0, c->stream>>>(d);
     F3CHECK(c);

@@ -11,8 +11,8 @@
 //
 // Algorithms: Knuth's TwoSum and Dekker's FastTwoSum for error-free sums, the
 // FMA-based TwoProduct for error-free products (Dekker 1971; Knuth, TAOCP vol. 2,
-// 4.2.2), the square root as one Newton correction of the FP32 root (Karp and
-// Markstein 1997).  The round-to-nearest intrinsics keep the compiler from contracting
+// 4.2.2), division as the FP32 quotient plus one remainder correction, the square
+// root as one Newton correction of the FP32 root (Karp and Markstein 1997).  The round-to-nearest intrinsics keep the compiler from contracting
 // the error-free transformations into fused multiply-adds.
 #pragma once
 #include <cstdint>
@@ -88,6 +88,14 @@ __device__ __forceinline__ dd operator*(dd a, dd b)
     return fast_two_sum(p, e);
 }
 __device__ __forceinline__ dd &operator+=(dd &a, dd b) { return a = a + b; }
+// a / b: the FP32 quotient of the leading parts, corrected once by the remainder
+// a - q b formed in double-float (long division in two digits).
+__device__ __forceinline__ dd operator/(dd a, dd b)
+{
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const dd r = a - b * dd(q1, 0.0f);
+    return fast_two_sum(q1, __fdiv_rn(r.hi, b.hi));
+}
 __device__ __forceinline__ dd fma(dd a, dd b, dd c) { return a * b + c; }
 // exact scaling by a power of two (no overflow or underflow at the magnitudes used)
 __device__ __forceinline__ dd scale2(dd a, float p2) { return dd(__fmul_rn(a.hi, p2), __fmul_rn(a.lo, p2)); }
