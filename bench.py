@@ -418,9 +418,12 @@ def make_ctx3(w, precision, device, g, du, dv, dw):
 def roofline_sweep3d(n_int, ms_per_launch, peaks, mixed):
     """Roofline of the 3-D Poisson line kernel from its average launch time (one
     colour = half the I lines).  Algorithmic bytes per active cell:
-    FP32 (k3_line32): RF, ANf, ASf, ATf, ABf, invDf, faf, fbf read, DF written, the
-    other colour's DF read once: 40 B.  FP64 (k3_line): SU, AN, AS, AT, AB, invD,
-    fa, fb read, P written, the other colour's P read once: 80 B."""
+    FP32 (k3_line32): RF, the north and top couplings of its own lines and of the
+    south and bottom neighbour lines (ANf, ATf: the operator is symmetric), invDf,
+    faf, fbf read, DF written, the other colour's DF read once: 40 B (the two colour
+    launches of a sweep share the coupling arrays, 8 B of the 40, through L2).
+    FP64 (k3_line): SU, AN, AS, AT, AB, invD, fa, fb read, P written, the other
+    colour's P read once: 80 B."""
     if not ms_per_launch or ms_per_launch <= 0:
         return None
     per_launch = (40.0 if mixed else 80.0) * (n_int // 2)
@@ -573,7 +576,7 @@ def run_les3d_bench(args):
     out = {
         "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["mixed"]["ms"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32pair+f32", "data": "synthetic",
         "config": {"workload": w["name"], "grid": f"{w['n_theta']} theta x {w['n_r']} r x {w['n_z']} z cells",
                    "cells": n_int, "re": w["re"], "dt": w["dt"], "lz": "pi", "dr1": w["dr1"],
                    "les": "dynamic Smagorinsky, coefficient averaged over the volume (the reference's); the "
@@ -582,8 +585,10 @@ def run_les3d_bench(args):
                    "poisson": f"red-black I-line GS to scaled-L1 {w['resimax']:g}, cap NSWPP={w['nswpp']}",
                    "sweeps_per_step": res["mixed"]["sweeps"],
                    "precision": f"mixed: FP32 red-black Poisson sweeps in FP64 refinement every "
-                                f"{w['refine_sweeps']} sweeps; metrics, residuals, predictor, SGS model and "
-                                "state FP64",
+                                f"{w['refine_sweeps']} sweeps; SGS model, DIF, NL, P_SOURCE, the AF right-hand "
+                                "sides and predictor line solves in double-float (FP32 pairs, ~48-bit "
+                                "significands); metrics, Poisson residual, divergence, CALCCOEF and the state "
+                                "FP64",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "256 MiB buffer written between timed steps (outside the events)"},
         "fp64": {"value": fp64_value, "ms_per_step": res["fp64"]["ms"] / args.steps,

@@ -95,7 +95,9 @@ struct D3 {
     LineDD sysd[6];   // mixed path: the factors of the six predictor sets as (hi, lo) pairs
     // MIXED Poisson: FP32 residual and correction, FP32 copies of the transverse
     // couplings of the Poisson set
-    float *RF, *DF, *ANf, *ASf, *ATf, *ABf;
+    // (the Poisson operator is symmetric: AS(j) = AN(j-1) and AB(k) = AT(k-1), the
+    // south and bottom couplings are read as the neighbours' north and top ones)
+    float *RF, *DF, *ANf, *ATf;
     // SGS model: two banks of 12 arrays for the separable test filters
     double *FB;
     // reductions
@@ -1070,7 +1072,7 @@ __device__ bool grid_sum3(const D3 &d, double &a, double &b, double &e, double *
     return true;
 }
 
-__global__ void __launch_bounds__(256) k3_pres(D3 d, Coef3 cf, int per)
+__global__ void __launch_bounds__(256) k3_pres(D3 d, Coef3 cf, int per, cudaGraphConditionalHandle cond)
 {
     __shared__ double sh[3 * 8];
     __shared__ bool last;
@@ -1096,6 +1098,7 @@ __global__ void __launch_bounds__(256) k3_pres(D3 d, Coef3 cf, int per)
         if (!(resip > d.resimax && it < d.nswpp)) {
             d.pctl->done = 1;
             d.pctl->capped = resip > d.resimax ? 1 : 0;
+            cudaGraphSetConditional(cond, 0);   // ends the device-side Poisson loop
         }
     }
 }
@@ -1140,12 +1143,10 @@ __global__ void k3_coef_f32(D3 d)
     if (c >= d.n) return;
     const Coef3 &cf = d.cf[6];
     d.ANf[c] = (float)cf.AN[c];
-    d.ASf[c] = (float)cf.AS[c];
     d.ATf[c] = (float)cf.AT[c];
-    d.ABf[c] = (float)cf.AB[c];
 }
 
-__global__ void __launch_bounds__(256) k3_mres(D3 d)
+__global__ void __launch_bounds__(256) k3_mres(D3 d, cudaGraphConditionalHandle cond)
 {
     __shared__ double sh[3 * 8];
     __shared__ bool last;
@@ -1174,15 +1175,29 @@ __global__ void __launch_bounds__(256) k3_mres(D3 d)
         if (it > 0 && !(resip > d.resimax && it < d.nswpp)) {
             d.pctl->done = 1;
             d.pctl->capped = resip > d.resimax ? 1 : 0;
+            cudaGraphSetConditional(cond, 0);   // ends the device-side Poisson loop
         } else {
             d.pctl->niter = it + d.refine_sweeps;
         }
     }
 }
 
-// One colour of the FP32 correction sweep on the I lines of the Poisson set.
+// BCP ghosts of the I line (j, k) of P (bcp.f90:24-34): P(0) = P(1), P(NI) cubic.
+__device__ __forceinline__ void line_bcp(const D3 &d, int j, int k)
+{
+    double *P = d.P;
+    P[ID3(0, j, k)] = P[ID3(1, j, k)];
+    P[ID3(d.NI, j, k)] = (3.0 * P[ID3(d.NI - 1, j, k)] - 3.0 * P[ID3(d.NI - 2, j, k)]) + P[ID3(d.NI - 3, j, k)];
+}
+
+// One colour of the FP32 correction sweep on the I lines of the Poisson set.  The
+// south and bottom couplings are the north and top couplings of the neighbouring
+// lines.  apply != 0 (the colour-1 launch of the last sweep of an outer iteration):
+// the group also adds the correction to P on its own line and on its colour-0
+// partner line (j-1, k) -- j -> j-1 maps the colour-1 lines of a plane one to one
+// onto the colour-0 lines -- and sets the BCP ghosts of both lines.
 template <int M, int NW>
-__global__ void __launch_bounds__(128) k3_line32(D3 d, LineSys s, int colour, int check_done)
+__global__ void __launch_bounds__(128) k3_line32(D3 d, LineSys s, int colour, int check_done, int apply)
 {
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ float sm[G][TG * M + M * NW + 1];
@@ -1203,8 +1218,8 @@ __global__ void __launch_bounds__(128) k3_line32(D3 d, LineSys s, int colour, in
         v[q] = 0.0f;
         if (active && e < n) {
             const int i = e + 1, c = ID3(i, j, k);
-            v[q] = ((d.ANf[c] * DF[ID3(i, jn, k)] + d.ASf[c] * DF[ID3(i, js, k)]) +
-                    (d.ATf[c] * DF[ID3(i, j, kt)] + d.ABf[c] * DF[ID3(i, j, kb)])) + d.RF[c];
+            v[q] = ((d.ANf[c] * DF[ID3(i, jn, k)] + d.ANf[ID3(i, js, k)] * DF[ID3(i, js, k)]) +
+                    (d.ATf[c] * DF[ID3(i, j, kt)] + d.ATf[ID3(i, j, kb)] * DF[ID3(i, j, kb)])) + d.RF[c];
         }
     }
     fvm::to_chunks<float, M, NW>(v, sm[gib], t);
@@ -1216,15 +1231,23 @@ __global__ void __launch_bounds__(128) k3_line32(D3 d, LineSys s, int colour, in
         const int e = q * TG + t;
         if (active && e < n) d.DF[ID3(e + 1, j, k)] = v[q];
     }
+    if (!apply) return;
+#pragma unroll
+    for (int q = 0; q < M; q++) {
+        const int e = q * TG + t;
+        if (active && e < n) {
+            d.P[ID3(e + 1, j, k)] += fvm::f2d_int(v[q]);
+            d.P[ID3(e + 1, js, k)] += fvm::f2d_int(DF[ID3(e + 1, js, k)]);
+        }
+    }
+    fvm::gsync<NW>();
+    if (active && t == 0) {
+        __threadfence_block();
+        line_bcp(d, j, k);
+        line_bcp(d, js, k);
+    }
 }
 
-__global__ void k3_apply(D3 d)
-{
-    CELL3(1, d.NI - 1, 1, d.NJ - 1, 1, d.NK - 1)
-    if (d.pctl->done) return;
-    const int c = ID3(i, j, k);
-    d.P[c] = d.P[c] + (double)d.DF[c];
-}
 
 }  // namespace f3
 
@@ -1933,7 +1956,7 @@ void carve(Bump &b, fvm3_ctx *c)
             sd.sinv = ls.cyclic ? reinterpret_cast<dd *>(b.take(F.lines)) : nullptr;
         }
     }
-    float **f32[] = {&d.RF, &d.DF, &d.ANf, &d.ASf, &d.ATf, &d.ABf};
+    float **f32[] = {&d.RF, &d.DF, &d.ANf, &d.ATf};
     for (auto p : f32) *p = reinterpret_cast<float *>(b.take((n + 1) / 2));
     d.FB = b.take(24 * n);
     d.nblk = 8 * 152;   // residual and reduction kernels: 8 blocks of 256 threads per SM
@@ -2038,7 +2061,7 @@ int line(fvm3_ctx *c, int set, const double *SU, double *phi, int colour, const 
     return FVM_OK;
 }
 
-int line32(fvm3_ctx *c, int colour, int check_done)
+int line32(fvm3_ctx *c, int colour, int check_done, int apply)
 {
     const D3 &d = c->d;
     const LineSys &s = d.sys[6];
@@ -2046,7 +2069,7 @@ int line32(fvm3_ctx *c, int colour, int check_done)
     const int blocks = fvm::line_blocks(per, s.NW);
     bool ok = fvm::dispatch_line(s, [&](auto m, auto nw) {
         constexpr int M = decltype(m)::value, NW = decltype(nw)::value;
-        k3_line32<M, NW><<<blocks, 128, 0, c->stream>>>(d, s, colour, check_done);
+        k3_line32<M, NW><<<blocks, 128, 0, c->stream>>>(d, s, colour, check_done, apply);
     });
     if (!ok) {
         c->err = "line length above 512 cells is not supported";
@@ -2156,18 +2179,35 @@ int poisson_graph(fvm3_ctx *c)
     D3 &d = c->d;
     const bool mixed = c->p.precision == FVM_MIXED;
     const int per = mixed ? d.refine_sweeps : d.res_every, groups = std::max(1, 32 / per);
+    // a device-side while loop: the residual kernel clears the condition when the
+    // iteration has converged or reached the cap, so no host synchronisation
     cudaGraph_t g = nullptr;
-    F3CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    F3CUDA(c, cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(c->stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        c->err = std::string("Poisson loop node: ") + cudaGetErrorString(e);
+        return FVM_ERR_CUDA;
+    }
     int rc = FVM_OK;
     for (int q = 0; q < groups && rc == FVM_OK && mixed; q++) {
         // residual (ends the loop), FP32 correction sweeps, P += dP, ghosts
-        k3_mres<<<d.nblk, 256, 0, c->stream>>>(d);
+        k3_mres<<<d.nblk, 256, 0, c->stream>>>(d, h);
         for (int it = 0; it < per && rc == FVM_OK; it++) {
-            rc = line32(c, 0, 1);
-            if (rc == FVM_OK) rc = line32(c, 1, 1);
+            rc = line32(c, 0, 1, 0);
+            if (rc == FVM_OK) rc = line32(c, 1, 1, it == per - 1);   // the last one adds dP and the BCP ghosts
         }
-        k3_apply<<<g_int(c), B_INT, 0, c->stream>>>(d);
-        k3_bcp<<<dim3((c->NJ + 127) / 128, c->NK + 1), 128, 0, c->stream>>>(d, 1);
         if (rc == FVM_OK) rc = halo(c, {d.P});
     }
     for (int q = 0; q < groups && rc == FVM_OK && !mixed; q++) {
@@ -2178,11 +2218,12 @@ int poisson_graph(fvm3_ctx *c)
             if (rc == FVM_OK) rc = line(c, 6, d.SU, d.P, 0, d.pctl);
             if (rc == FVM_OK) rc = line(c, 6, d.SU, d.P, 1, d.pctl);
         }
-        k3_pres<<<d.nblk, 256, 0, c->stream>>>(d, d.cf[6], per);
+        k3_pres<<<d.nblk, 256, 0, c->stream>>>(d, d.cf[6], per, h);
     }
-    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamEndCapture(c->stream, &body);
     if (rc || e != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
+        cudaGraphDestroy(g);
         if (!rc) c->err = std::string("Poisson capture: ") + cudaGetErrorString(e);
         return rc ? rc : FVM_ERR_CUDA;
     }
@@ -2201,17 +2242,9 @@ int poisson(fvm3_ctx *c)
     D3 &d = c->d;
     F3RC(poisson_graph(c));
     k3_pctl_reset<<<1, 1, 0, c->stream>>>(d);
-    const long max_launches = (long)d.nswpp / c->pgraph_iters + 2;
-    for (long l = 0;; l++) {
-        if (l >= max_launches) {
-            c->err = "Poisson iteration did not report completion within the sweep cap";
-            return FVM_ERR_TIMEOUT;
-        }
-        F3CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
-        F3CUDA(c, cudaMemcpyAsync(c->h_pctl, d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
-        F3CUDA(c, cudaStreamSynchronize(c->stream));
-        if (c->h_pctl->done) break;
-    }
+    // one launch: the loop runs on the device until the residual kernel ends it (the
+    // sweep cap bounds it); the statistics stay on the device for CALCCOEF
+    F3CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
     return FVM_OK;
 }
 
@@ -2837,8 +2870,8 @@ int fvm3_time_sweeps(fvm3_ctx *c, int sweeps, double *ms_per_sweep)
     const bool mixed = c->p.precision == FVM_MIXED;
     for (int s = 0; s < sweeps && rc == FVM_OK; s++) {
         if (mixed) {
-            rc = f3::line32(c, 0, 0);
-            if (rc == FVM_OK) rc = f3::line32(c, 1, 0);
+            rc = f3::line32(c, 0, 0, 0);
+            if (rc == FVM_OK) rc = f3::line32(c, 1, 0, 0);
         } else {
             rc = f3::line(c, 6, d.SU, d.DIVDT, 0);
             if (rc == FVM_OK) rc = f3::line(c, 6, d.SU, d.DIVDT, 1);

@@ -32,9 +32,12 @@ typedef struct fvm3_params {
     int res_every;         /* Poisson residual every k-th sweep */
     double ref_a;          /* reference area of the force coefficients (REF_A) */
     int precision;         /* FVM_FP64, or FVM_MIXED: FP32 red-black Poisson sweeps on the
-                              correction inside FP64 residual refinement; everything else
-                              (metrics, residuals, predictor, the SGS model, whose Leonard
-                              term cancels to ~1e-6 of its operands, and the state) FP64 */
+                              correction inside FP64 residual refinement; the SGS model, DIF,
+                              NL, P_SOURCE, the AF right-hand sides and predictor line solves
+                              in double-float (pairs of FP32, ~48-bit significands: the
+                              Leonard term cancels to ~1e-6 of its operands, too far for
+                              FP32); metrics, the Poisson residual, divergence, CALCCOEF and
+                              the state FP64 */
     int refine_sweeps;     /* MIXED: FP32 sweeps per FP64 residual */
     int device;
     int tile_i_warps, tile_i_m;   /* tile of the I lines (Poisson and first AF sweep), 0 = automatic:
