@@ -23,7 +23,7 @@ class Params3(ctypes.Structure):
                 ("nswpp", ctypes.c_int), ("use_les", ctypes.c_int), ("les_zavg", ctypes.c_int),
                 ("thermal", ctypes.c_int), ("res_every", ctypes.c_int), ("ref_a", ctypes.c_double),
                 ("precision", ctypes.c_int), ("refine_sweeps", ctypes.c_int), ("device", ctypes.c_int),
-                ("tile_i_warps", ctypes.c_int), ("tile_i_m", ctypes.c_int)]
+                ("tile_i_warps", ctypes.c_int), ("tile_i_m", ctypes.c_int), ("poisson_host_loop", ctypes.c_int)]
 
 
 class Coeffs3(ctypes.Structure):

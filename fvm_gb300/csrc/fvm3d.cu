@@ -1072,6 +1072,10 @@ __device__ bool grid_sum3(const D3 &d, double &a, double &b, double &e, double *
     return true;
 }
 
+// HAS_COND: the device-loop form, which ends the graph while node; a separate
+// instantiation keeps the host-loop kernels free of device graph calls (profilers
+// skip kernels that contain them).
+template <int HAS_COND>
 __global__ void __launch_bounds__(256) k3_pres(D3 d, Coef3 cf, int per, cudaGraphConditionalHandle cond)
 {
     __shared__ double sh[3 * 8];
@@ -1098,7 +1102,7 @@ __global__ void __launch_bounds__(256) k3_pres(D3 d, Coef3 cf, int per, cudaGrap
         if (!(resip > d.resimax && it < d.nswpp)) {
             d.pctl->done = 1;
             d.pctl->capped = resip > d.resimax ? 1 : 0;
-            cudaGraphSetConditional(cond, 0);   // ends the device-side Poisson loop
+            if constexpr (HAS_COND) cudaGraphSetConditional(cond, 0);   // ends the device-side loop
         }
     }
 }
@@ -1146,6 +1150,7 @@ __global__ void k3_coef_f32(D3 d)
     d.ATf[c] = (float)cf.AT[c];
 }
 
+template <int HAS_COND>
 __global__ void __launch_bounds__(256) k3_mres(D3 d, cudaGraphConditionalHandle cond)
 {
     __shared__ double sh[3 * 8];
@@ -1175,7 +1180,7 @@ __global__ void __launch_bounds__(256) k3_mres(D3 d, cudaGraphConditionalHandle 
         if (it > 0 && !(resip > d.resimax && it < d.nswpp)) {
             d.pctl->done = 1;
             d.pctl->capped = resip > d.resimax ? 1 : 0;
-            cudaGraphSetConditional(cond, 0);   // ends the device-side Poisson loop
+            if constexpr (HAS_COND) cudaGraphSetConditional(cond, 0);   // ends the device-side loop
         } else {
             d.pctl->niter = it + d.refine_sweeps;
         }
@@ -2179,31 +2184,39 @@ int poisson_graph(fvm3_ctx *c)
     D3 &d = c->d;
     const bool mixed = c->p.precision == FVM_MIXED;
     const int per = mixed ? d.refine_sweeps : d.res_every, groups = std::max(1, 32 / per);
-    // a device-side while loop: the residual kernel clears the condition when the
-    // iteration has converged or reached the cap, so no host synchronisation
+    // host loop: the graph is one body, replayed until the control block reports
+    // completion; device loop: a while node whose condition the residual kernel
+    // clears when the iteration has converged or reached the cap
+    const int dev_loop = c->p.poisson_host_loop ? 0 : 1;
     cudaGraph_t g = nullptr;
-    F3CUDA(c, cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle h;
-    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphConditionalHandle h = 0;
     cudaGraphNodeParams cp = {};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = h;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t node;
-    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
-    if (e == cudaSuccess)
-        e = cudaStreamBeginCaptureToGraph(c->stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                          cudaStreamCaptureModeThreadLocal);
+    cudaError_t e = cudaSuccess;
+    if (dev_loop) {
+        F3CUDA(c, cudaGraphCreate(&g, 0));
+        e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(c->stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+    } else {
+        e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    }
     if (e != cudaSuccess) {
-        cudaGraphDestroy(g);
+        if (g) cudaGraphDestroy(g);
         c->err = std::string("Poisson loop node: ") + cudaGetErrorString(e);
         return FVM_ERR_CUDA;
     }
     int rc = FVM_OK;
     for (int q = 0; q < groups && rc == FVM_OK && mixed; q++) {
         // residual (ends the loop), FP32 correction sweeps, P += dP, ghosts
-        k3_mres<<<d.nblk, 256, 0, c->stream>>>(d, h);
+        if (dev_loop) k3_mres<1><<<d.nblk, 256, 0, c->stream>>>(d, h);
+        else k3_mres<0><<<d.nblk, 256, 0, c->stream>>>(d, h);
         for (int it = 0; it < per && rc == FVM_OK; it++) {
             rc = line32(c, 0, 1, 0);
             if (rc == FVM_OK) rc = line32(c, 1, 1, it == per - 1);   // the last one adds dP and the BCP ghosts
@@ -2218,12 +2231,14 @@ int poisson_graph(fvm3_ctx *c)
             if (rc == FVM_OK) rc = line(c, 6, d.SU, d.P, 0, d.pctl);
             if (rc == FVM_OK) rc = line(c, 6, d.SU, d.P, 1, d.pctl);
         }
-        k3_pres<<<d.nblk, 256, 0, c->stream>>>(d, d.cf[6], per, h);
+        if (dev_loop) k3_pres<1><<<d.nblk, 256, 0, c->stream>>>(d, d.cf[6], per, h);
+        else k3_pres<0><<<d.nblk, 256, 0, c->stream>>>(d, d.cf[6], per, h);
     }
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaGraph_t body = dev_loop ? cp.conditional.phGraph_out[0] : nullptr;
     e = cudaStreamEndCapture(c->stream, &body);
+    if (!dev_loop) g = body;
     if (rc || e != cudaSuccess) {
-        cudaGraphDestroy(g);
+        if (g) cudaGraphDestroy(g);
         if (!rc) c->err = std::string("Poisson capture: ") + cudaGetErrorString(e);
         return rc ? rc : FVM_ERR_CUDA;
     }
@@ -2242,9 +2257,23 @@ int poisson(fvm3_ctx *c)
     D3 &d = c->d;
     F3RC(poisson_graph(c));
     k3_pctl_reset<<<1, 1, 0, c->stream>>>(d);
-    // one launch: the loop runs on the device until the residual kernel ends it (the
-    // sweep cap bounds it); the statistics stay on the device for CALCCOEF
-    F3CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
+    if (!c->p.poisson_host_loop) {
+        // one launch: the loop runs on the device until the residual kernel ends it
+        // (the sweep cap bounds it); the statistics stay on the device for CALCCOEF
+        F3CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
+        return FVM_OK;
+    }
+    const long max_launches = (long)d.nswpp / c->pgraph_iters + 2;
+    for (long l = 0;; l++) {
+        if (l >= max_launches) {
+            c->err = "Poisson iteration did not report completion within the sweep cap";
+            return FVM_ERR_TIMEOUT;
+        }
+        F3CUDA(c, cudaGraphLaunch(c->pgraph, c->stream));
+        F3CUDA(c, cudaMemcpyAsync(c->h_pctl, d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
+        F3CUDA(c, cudaStreamSynchronize(c->stream));
+        if (c->h_pctl->done) break;
+    }
     return FVM_OK;
 }
 
@@ -2494,6 +2523,7 @@ int fvm3_default_params(fvm3_params *p)
     p->precision = FVM_FP64;
     p->refine_sweeps = 8;
     p->device = 0;
+    p->poisson_host_loop = 1;
     return FVM_OK;
 }
 

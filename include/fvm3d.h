@@ -44,6 +44,9 @@ typedef struct fvm3_params {
                                      warps per line group (1, 2, 4) and elements per thread
                                      (1..4; also 6, 8, 12 with one warp, 6, 8 with two);
                                      32 * warps * elements must cover NI-1 */
+    int poisson_host_loop; /* 1 (default): the host replays the Poisson body until the
+                              residual kernel reports completion (kernels visible to
+                              profilers); 0: a graph while-node ends the loop on the device */
 } fvm3_params;
 
 typedef struct fvm3_coeffs {
