@@ -146,8 +146,9 @@ def test_mixed_tracks_fp64_on_a_wall_resolved_grid():
     """On a grid with the first radial spacing of the LES configuration (0.001 D)
     the mixed path stays close to the FP64 path over several steps, and the flow
     stays bounded (the coefficient averaged over the volume, as the reference).
-    Both stop the Poisson iteration at the same sweep cap, so they differ by the
-    unconverged remainders (~1e-5), not by the precision of the stencils."""
+    Both stop the Poisson iteration at the same sweep cap; the mixed path's FP32
+    sweeps and double-float stencils leave ~1e-7 in the fields and ~1e-6 in the drag
+    (an FP32 SGS model, which loses the Leonard term, had changed Cd by 120 %)."""
     g = o_grid_3d(64, 48, 16, lz=np.pi, dr1=0.001)
     du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, 0.05, 0)
     out = {}
@@ -161,9 +162,9 @@ def test_mixed_tracks_fp64_on_a_wall_resolved_grid():
         c = ctx.step(6)
         out[prec] = ({nm: ctx.get(nm) for nm in ("U", "V", "W", "P", "T")}, c["cd"])
         ctx.close()
-    for nm in ("U", "V", "W", "T"):
-        assert rel_l2(out[capi.MIXED][0][nm], out[capi.FP64][0][nm]) <= 1e-3, nm
-    assert abs(out[capi.MIXED][1] - out[capi.FP64][1]) <= 1e-3 * abs(out[capi.FP64][1])
+    for nm in ("U", "V", "W", "P", "T"):
+        assert rel_l2(out[capi.MIXED][0][nm], out[capi.FP64][0][nm]) <= 1e-6, nm
+    assert abs(out[capi.MIXED][1] - out[capi.FP64][1]) <= 1e-5 * abs(out[capi.FP64][1])
     # bounded flow through the impulsive start (|u| stays near 2, the drag coefficient
     # swings within tens while the capped Poisson iteration settles)
     assert np.abs(out[capi.FP64][0]["U"]).max() < 3.0 and abs(out[capi.FP64][1]) < 50.0
