@@ -108,11 +108,18 @@ class ClockSampler:
 # ---------------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------------
+# The Poisson loop of a step: "device" (a graph while node ends it, no host round trip
+# per outer iteration) or "host" (the host replays the body until the control block
+# reports completion; ncu lists only the kernels of this form).  Set from --poisson-loop.
+POISSON_LOOP = {"mode": "device"}
+
+
 def make_ctx(w, precision, device, g, du, dv):
     from fvm_gb300 import capi
     p = capi.default_params(ni=g.ni, nj=g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], resimax=w["resimax"],
                             nswpp=w["nswpp"], thermal=w["thermal"], precision=precision,
-                            res_every=w["res_every"], refine_sweeps=w["refine_sweeps"], adi_refine=2, device=device)
+                            res_every=w["res_every"], refine_sweeps=w["refine_sweeps"], adi_refine=2, device=device,
+                            poisson_host_loop=1 if POISSON_LOOP["mode"] == "host" else 0)
     ctx = capi.Context(p)
     ctx.set_grid(g.xg, g.yg)
     ctx.init(du, dv)
@@ -278,6 +285,7 @@ def run_ours(args):
                    f"refinement every {w['refine_sweeps']} sweeps, FP32 predictor lines with 2 FP64 "
                    "defect-correction passes; state, metrics and residuals FP64",
                    "parallelism": "replicas" if world > 1 else "single GPU",
+                   "poisson_loop": POISSON_LOOP["mode"],
                    "l2": "256 MiB buffer written between timed steps (outside the events)"},
         "fp64": {"value": fp64_value, "ms_per_step": res["fp64"]["ms"] / args.steps,
                  "sweeps_per_step": res["fp64"]["sweeps"], "roofline": roof64},
@@ -408,7 +416,8 @@ def make_ctx3(w, precision, device, g, du, dv, dw):
     p = capi3d.default_params(ni=g.ni, nj=g.nj, nk=g.nk, re=w["re"], pr=w["pr"], dt=w["dt"], resimax=w["resimax"],
                               nswpp=w["nswpp"], use_les=1, les_zavg=w["zavg"], thermal=w["thermal"],
                               res_every=w["res_every"], refine_sweeps=w["refine_sweeps"], precision=precision,
-                              ref_a=float(g.zg[g.nk, 1, 1] - g.zg[1, 1, 1]), device=device)
+                              ref_a=float(g.zg[g.nk, 1, 1] - g.zg[1, 1, 1]), device=device,
+                              poisson_host_loop=1 if POISSON_LOOP["mode"] == "host" else 0)
     ctx = capi3d.Context3(p)
     ctx.set_grid(g)
     ctx.init(du, dv, dw)
@@ -590,6 +599,7 @@ def run_les3d_bench(args):
                                 "significands); metrics, Poisson residual, divergence, CALCCOEF and the state "
                                 "FP64",
                    "parallelism": "replicas" if world > 1 else "single GPU",
+                   "poisson_loop": POISSON_LOOP["mode"],
                    "l2": "256 MiB buffer written between timed steps (outside the events)"},
         "fp64": {"value": fp64_value, "ms_per_step": res["fp64"]["ms"] / args.steps,
                  "sweeps_per_step": res["fp64"]["sweeps"],
@@ -777,11 +787,15 @@ def main():
                          "adjoint: window-drag gradient on the 128x96 grid; "
                          "les3d: 3-D LES on the 256x192x48 grid, FP64 and mixed")
     ap.add_argument("--spinup", type=int, default=200, help="adjoint workload: steps before the window")
+    ap.add_argument("--poisson-loop", choices=["device", "host"], default="device",
+                    help="cylinder2d and les3d: the Poisson loop on the device (graph while node) or replayed by "
+                         "the host (kernels listed by ncu)")
     ap.add_argument("--les3d-grid", choices=["full", "profile"], default="full",
                     help="les3d: the 256x192x48 grid, or 192x160x32 for profiler captures")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    POISSON_LOOP["mode"] = args.poisson_loop
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "sweep64":

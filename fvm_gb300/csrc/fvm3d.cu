@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(128) k3_line(D3 d, LineSys s, Coef3 cf, const 
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ T sm[G][TG * M + M * NW + 1];
     __shared__ T xch[G][2 * NW];
-    if (stop && stop->done) return;   // the Poisson loop has ended
+    const int ended = stop ? stop->done : 0;   // the Poisson loop has ended (tested after the loads)
     int gl, t, gib;
     fvm::group_of<NW>(gl, t, gib);
     int L = 0;
@@ -693,6 +693,7 @@ __global__ void __launch_bounds__(128) k3_line(D3 d, LineSys s, Coef3 cf, const 
                                fma(lds<T>(d, c4, c), lds<T>(d, phi, c + g.o4), ld<T>(SU[c])))));
         }
     }
+    if (ended) return;
     fvm::to_chunks<T, M, NW>(v, sm[gib], t);
     const size_t base = size_t(L) * TG * M;
     if constexpr (std::is_same<T, double>::value) {
@@ -1243,7 +1244,8 @@ __global__ void __launch_bounds__(128) k3_line32(D3 d, LineSys s, int colour, in
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ float sm[G][TG * M + M * NW + 1];
     __shared__ float xch[G][2 * NW];
-    if (check_done && d.pctl->done) return;
+    // the loop's done flag is loaded together with the operands below
+    const int stop = check_done ? d.pctl->done : 0;
     int gl, t, gib;
     fvm::group_of<NW>(gl, t, gib);
     int L = 0;
@@ -1263,6 +1265,7 @@ __global__ void __launch_bounds__(128) k3_line32(D3 d, LineSys s, int colour, in
                     (d.ATf[c] * DF[ID3(i, j, kt)] + d.ATf[ID3(i, j, kb)] * DF[ID3(i, j, kb)])) + d.RF[c];
         }
     }
+    if (stop) return;
     fvm::to_chunks<float, M, NW>(v, sm[gib], t);
     const size_t base = size_t(L) * TG * M;
     fvm::group_apply<float, M, NW>(v, s.invDf + base, s.faf + base, s.fbf + base, t, xch[gib]);

@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(128) k_adj_pois(Dev d, Adj a, int colour)
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ double sm[G][TG * M + M * NW + 1];
     __shared__ double xch[G][2 * NW];
-    if (a.pctl->done) return;
+    const int stop = a.pctl->done;   // tested after the operand loads
     int gl, t, gib;
     group_of<NW>(gl, t, gib);
     const bool active = gl < (d.NJ - 1) / 2;
@@ -591,6 +591,7 @@ __global__ void __launch_bounds__(128) k_adj_pois(Dev d, Adj a, int colour)
             v[k] = ((cf.AN[c] * a.mu[IDX(e + 1, jn)] + cf.AS[c] * a.mu[IDX(e + 1, js)]) + a.g[c]) - a.XD[c];
         }
     }
+    if (stop) return;
     to_chunks<double, M, NW>(v, sm[gib], t);
     const size_t base = size_t(j - 1) * TG * M;
     group_apply<double, M, NW>(v, s.invD + base, s.fa + base, s.fb + base, t, xch[gib]);
@@ -692,7 +693,7 @@ __global__ void __launch_bounds__(128) k_adj_pois32(Dev d, Adj a, int colour)
     constexpr int TG = WARP * NW, G = 4 / NW;
     __shared__ float sm[G][TG * M + M * NW + 1];
     __shared__ float xch[G][2 * NW];
-    if (a.pctl->done) return;
+    const int stop = a.pctl->done;   // tested after the operand loads
     int gl, t, gib;
     group_of<NW>(gl, t, gib);
     const bool active = gl < (d.NJ - 1) / 2;
@@ -711,6 +712,7 @@ __global__ void __launch_bounds__(128) k_adj_pois32(Dev d, Adj a, int colour)
             v[k] = (cf.ANf[c] * d.DF[IDX(e + 1, jn)] + cf.ASf[c] * d.DF[IDX(e + 1, js)]) + d.RF[c];
         }
     }
+    if (stop) return;
     to_chunks<float, M, NW>(v, sm[gib], t);
     const size_t base = size_t(j - 1) * TG * M;
     group_apply<float, M, NW>(v, s.invDf + base, s.faf + base, s.fbf + base, t, xch[gib]);

@@ -93,7 +93,9 @@ __global__ void __launch_bounds__(128) k_pois32(const __grid_constant__ S src, i
         as[k] = ok ? cf.ASf[IDX(e + 1, j)] : 0.0f;
     }
     griddep_wait();
-    if (check_done && d.pctl->done) return;
+    // the loop's done flag is loaded together with the operands (a separate load
+    // before them put one more L2 round trip on every launch's critical path)
+    const int stop = check_done ? d.pctl->done : 0;
     float v[M];
 #pragma unroll
     for (int k = 0; k < M; k++) {
@@ -104,6 +106,7 @@ __global__ void __launch_bounds__(128) k_pois32(const __grid_constant__ S src, i
             v[k] = (an[k] * d.DF[IDX(i, jn)] + as[k] * d.DF[IDX(i, js)]) + d.RF[IDX(i, j)];
         }
     }
+    if (stop) return;
     griddep_launch();   // the next sweep may start its constant prologue now
     to_chunks<float, M, NW>(v, sm[gib], t);
     group_apply_r<float, M, NW>(v, fi, fa, fb, t, xch[gib]);

@@ -395,11 +395,9 @@ __global__ void __launch_bounds__(128) k_pois64(const __grid_constant__ S src, i
         dv[k] = ok ? d.DIVDT[c] : 0.0;
     }
     griddep_wait();
-    if (check_done && d.pctl->done) return;
-    if (active && colour == 0 && t < WARP) {   // BCP of this iteration: ghosts of P^(n-1), stored with P^n
-        refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j, nullptr, nullptr, t);
-        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j + 1, nullptr, nullptr, t);
-    }
+    // the loop's done flag is loaded together with the operands (a separate load
+    // before them put one more L2 round trip on every launch's critical path)
+    const int stop = check_done ? d.pctl->done : 0;
     const double *Pnb = colour ? Pout : Pin;
     double v[M];
 #pragma unroll
@@ -411,6 +409,13 @@ __global__ void __launch_bounds__(128) k_pois64(const __grid_constant__ S src, i
             double su = dv[k] - dd_src(d, Pin, i, j);
             v[k] = (an[k] * Pnb[IDX(i, jn)] + as[k] * Pnb[IDX(i, js)]) + su;
         }
+    }
+    if (stop) return;
+    // BCP of this iteration: ghosts of P^(n-1), stored with P^n (colour 0 reads only
+    // P^(n-1), so the ghosts of P^n may follow its loads)
+    if (active && colour == 0 && t < WARP) {
+        refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j, nullptr, nullptr, t);
+        if (j + 1 <= d.NJ - 1) refresh_row_ghosts<BCK_POISSON>(d, Pin, Pout, j + 1, nullptr, nullptr, t);
     }
     griddep_launch();   // the next kernel may start its constant prologue now
     to_chunks<double, M, NW>(v, sm[gib], t);

@@ -207,3 +207,24 @@ def test_mixed_predictor_single_pass_is_fp32_accurate():
     e1 = rel_l2(one.get("U"), ref.get("U"), (g.ni, g.nj))
     e2 = rel_l2(two.get("U"), ref.get("U"), (g.ni, g.nj))
     assert e2 <= 1e-12 and e2 < e1 <= 1e-6
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED], ids=["fp64", "mixed"])
+def test_device_poisson_loop_equals_host_loop(precision):
+    """The graph while-node Poisson loop (poisson_host_loop = 0) runs the same kernels
+    in the same order as the host replay: identical fields, coefficients and sweeps."""
+    case = make_case(32, 24, re=200.0, dt=0.002, resimax=1e-10, nswpp=3000)
+    out = []
+    for host_loop in (1, 0):
+        g = case["g"]
+        p = capi.default_params(ni=g.ni, nj=g.nj, re=200.0, pr=0.71, dt=0.002, resimax=1e-10, nswpp=3000,
+                                thermal=1, precision=precision, poisson_host_loop=host_loop)
+        ctx = capi.Context(p)
+        ctx.set_grid(g.xg, g.yg)
+        ctx.init(case["du"], case["dv"])
+        co = [ctx.step(1) for _ in range(3)]
+        out.append(([(c["sweeps"], c["cd"]) for c in co], {nm: ctx.get(nm) for nm in ("U", "V", "P", "T")}))
+        ctx.close()
+    assert out[0][0] == out[1][0]
+    for nm in ("U", "V", "P", "T"):
+        assert np.array_equal(out[0][1][nm], out[1][1][nm]), nm
