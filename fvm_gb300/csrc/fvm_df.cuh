@@ -87,7 +87,6 @@ __device__ __forceinline__ dd operator*(dd a, dd b)
     e = __fmaf_rn(a.lo, b.hi, e);
     return fast_two_sum(p, e);
 }
-__device__ __forceinline__ dd &operator+=(dd &a, dd b) { return a = a + b; }
 // a / b: the FP32 quotient of the leading parts, corrected once by the remainder
 // a - q b formed in double-float (long division in two digits).
 __device__ __forceinline__ dd operator/(dd a, dd b)
