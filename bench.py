@@ -14,8 +14,9 @@ value: the mixed-precision path (FP32 zebra sweeps in FP64 refinement); the FP64
 path is timed in the same run.  e2e: the same metric through the C-ABI with the
 state uploaded from and downloaded to pinned host memory every step.
 
---impl reference times the CPU restatement of the reference (serial, the
-reference's execution model) on the same workload.
+--impl reference times the CPU restatement of the reference in its own order
+(line sweeps sequential, as the reference's; stencil loops on every host thread)
+on the same workload.
 """
 from __future__ import annotations
 
@@ -143,12 +144,20 @@ def timed_steps(ctx, steps, flush, torch, ext):
     return total
 
 
-def cpu_baseline(w, g, du, dv, steps=2):
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(w, g, du, dv, steps=3):
     """Serial CPU restatement (reference order) on a bounded sample: the first
-    `steps` steps of the same workload."""
+    `steps` steps of the same workload, timing build of the restatement (-O3 with
+    FMA contraction; portable flags, no -march=native)."""
     import oracle
     o = oracle.Oracle(g.ni, g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], order=oracle.FAITHFUL,
-                      resimax=w["resimax"], nswpp=w["nswpp"], thermal=bool(w["thermal"]))
+                      resimax=w["resimax"], nswpp=w["nswpp"], thermal=bool(w["thermal"]), variant="fast")
     o.set_grid(g.xg, g.yg)
     o.init(du, dv)
     t0 = time.perf_counter()
@@ -157,7 +166,42 @@ def cpu_baseline(w, g, du, dv, steps=2):
     sw = o.coeffs()["sweeps"]
     return {"value": cells(w) * steps / dt / 1e6, "unit": "Mcell-steps/s", "cores": 1, "kind": "port",
             "sample": f"first {steps} time steps of the same workload ({sw} Poisson sweeps in the last), "
-                      f"serial restatement in the reference's lexicographic order, {dt:.1f} s"}
+                      f"serial restatement in the reference's lexicographic order (-O3, FMA contraction), "
+                      f"{dt:.1f} s"}
+
+
+def oracle_gpu_order(w, g, du, dv, steps):
+    """The restatement in GPU order (zebra sweeps, periodic wrap, cyclic circumferential
+    lines) over the same `steps` steps, sweep cap and residual interval as the FP64
+    GPU path, on all host threads (the OpenMP build, bit-identical to the serial
+    checker).  Returns the final fields, the last step's coefficients and the time."""
+    import oracle
+    o = oracle.Oracle(g.ni, g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], order=oracle.GPU, resimax=w["resimax"],
+                      nswpp=w["nswpp"], thermal=bool(w["thermal"]), res_every=w["res_every"], variant="par")
+    o.set_grid(g.xg, g.yg)
+    o.init(du, dv)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    return {nm: o.array(nm).copy() for nm in ("U", "V", "P", "T")}, o.coeffs(), dt
+
+
+def vs_oracle(res, ofields, oco, w):
+    """rel-L2 of the fields and relative coefficient errors of each GPU path against
+    the GPU-order restatement after the same steps."""
+    import numpy as np
+    ni, nj = w["n_r"] + 1, w["n_theta"] + 1
+
+    def rel(a, b):
+        a, b = a[1:nj, 1:ni], b[1:nj, 1:ni]
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    out = {}
+    for path, r in res.items():
+        out[path] = {"field_rel_l2": {nm: rel(r["fields"][nm], ofields[nm]) for nm in ("U", "V", "P", "T")},
+                     "coeff_rel": {k: abs(r[k] - oco[k]) / abs(oco[k]) for k in ("cd", "cl", "nu")},
+                     "sweeps": {"gpu": r["sweeps"], "oracle": oco["sweeps"]}}
+    return out
 
 
 def roofline_sweep(w, ms_per_launch, peaks, mixed):
@@ -222,7 +266,8 @@ def run_ours(args):
         hist = ctx.history(1)
         fields = {nm: ctx.get(nm).copy() for nm in ("U", "V", "P", "T")}
         res[name] = dict(ms=ms_max, timing=tm, clocks=clocks, sweeps=hist[0]["sweeps"], fields=fields,
-                         cd=hist[0]["cd"], resid=hist[0]["resid"], sweep_ms=sweep_ms)
+                         cd=hist[0]["cd"], cl=hist[0]["cl"], nu=hist[0]["nu"], resid=hist[0]["resid"],
+                         sweep_ms=sweep_ms)
         ctx.close()
 
     if args.parts == "mixed":   # profiling runs: the headline path only
@@ -299,6 +344,19 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(w, g, du, dv)
+        # the GPU-order restatement over the same warm-up + timed steps: the parity
+        # of both GPU paths at this configuration, and a second (labelled) CPU figure
+        nst = args.warmup + args.steps
+        ofields, oco, odt = oracle_gpu_order(w, g, du, dv, nst)
+        out["vs_oracle"] = vs_oracle({"mixed": res["mixed"], "fp64": res["fp64"]}, ofields, oco, w)
+        out["vs_oracle"]["steps"] = nst
+        out["vs_oracle"]["oracle"] = (f"CPU restatement in GPU order, residual every {w['res_every']} sweeps, "
+                                      f"cap {w['nswpp']}, the same {nst} steps from the same inputs")
+        out["cpu_gpu_order_omp"] = {
+            "value": cells(w) * nst / odt / 1e6, "unit": "Mcell-steps/s", "cores": host_threads(), "kind": "port",
+            "sample": f"{nst} steps of the workload, restatement in GPU order (zebra sweeps of one colour and "
+                      f"the stencil loops on {host_threads()} OpenMP threads), {odt:.1f} s; not the reference's "
+                      f"order, reported beside the serial baseline"}
     elif rank == 0:
         out["cpu_baseline"] = None
     if rank == 0:
@@ -715,8 +773,11 @@ def run_reference(args):
     import oracle
     w = dict(WORKLOAD)
     g, du, dv = case_inputs(w)
+    # The reference's algorithm: lexicographic line Gauss-Seidel, sequential over the
+    # lines; the OpenMP build runs its stencil loops on every host thread (results
+    # bit-identical to the serial restatement).
     o = oracle.Oracle(g.ni, g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], order=oracle.FAITHFUL,
-                      resimax=w["resimax"], nswpp=w["nswpp"], thermal=bool(w["thermal"]))
+                      resimax=w["resimax"], nswpp=w["nswpp"], thermal=bool(w["thermal"]), variant="par")
     o.set_grid(g.xg, g.yg)
     o.init(du, dv)
     # Each step is timed by sub-step so that a long run can sample fewer Poisson
@@ -743,7 +804,7 @@ def run_reference(args):
     def rebuild(cap):
         nonlocal o
         o = oracle.Oracle(g.ni, g.nj, re=w["re"], pr=w["pr"], dt=w["dt"], order=oracle.FAITHFUL,
-                          resimax=w["resimax"], nswpp=cap, thermal=bool(w["thermal"]))
+                          resimax=w["resimax"], nswpp=cap, thermal=bool(w["thermal"]), variant="par")
         o.set_grid(g.xg, g.yg)
         o.init(du, dv)
 
@@ -760,7 +821,8 @@ def run_reference(args):
         tf, tp, swn = one_step(sample_sweeps)
         tot += tf + tp * (w["nswpp"] / max(swn, 1))
     value = cells(w) * args.steps / tot / 1e6
-    sample = (f"CPU restatement, reference (lexicographic) order, serial; {args.steps} steps of the workload"
+    sample = (f"CPU restatement, reference (lexicographic) order: line sweeps sequential as in the reference, "
+              f"stencil loops on {host_threads()} OpenMP threads; {args.steps} steps of the workload"
               + ("" if sample_sweeps == w["nswpp"] else
                  f", Poisson sampled at {sample_sweeps} of {w['nswpp']} sweeps per step and scaled"))
     out = {"metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": world, "steps": args.steps,
@@ -768,7 +830,8 @@ def run_reference(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
            "config": {"workload": w["name"], "cells": cells(w),
                       "poisson": f"line GS to scaled-L1 {w['resimax']:g}, cap NSWPP={w['nswpp']}"},
-           "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": 1, "kind": "port", "sample": sample},
+           "cpu_baseline": {"value": value, "unit": "Mcell-steps/s", "cores": host_threads(), "kind": "port",
+                            "sample": sample},
            "e2e": {"value": value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

@@ -77,7 +77,9 @@ std::mutex g_mu;
 void *g_addr[64] = {};
 
 // Device address of the static scratch on the current device (set up once per
-// device, with that device current).
+// device, with that device current).  The address is kept for the life of the
+// process: a cudaDeviceReset (or any other teardown of the device's primary
+// context) unmaps it, so the library must not be used across a device reset.
 cudaError_t scratch_address(int dev, double **ptr)
 {
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
@@ -98,10 +100,11 @@ extern "C" int fvm_poisson_residual_static(int ni, int nj, const double *p, cons
                                            const double *ae, const double *aw, const double *an,
                                            const double *as, double *resid, void *stream)
 {
-    if (!p || !su || !ap || !ae || !aw || !an || !as || !resid) return FVM_ERR_ARG;
+    // sizes first: an oversized grid is refused before any pointer is looked at
     if (ni < 3 || nj < 3) return FVM_ERR_ARG;
     const long long cells = (long long)(ni - 1) * (nj - 1);
     if (cells > kMaxCells) return FVM_ERR_ARG;
+    if (!p || !su || !ap || !ae || !aw || !an || !as || !resid) return FVM_ERR_ARG;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return FVM_ERR_CUDA;
     double *scratch = nullptr;

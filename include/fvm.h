@@ -226,7 +226,9 @@ int fvm_time_sweeps(struct fvm_ctx *ctx, int sweeps, double *ms_per_launch, long
  * call on a device resolves the scratch address (once per device, with that device
  * current) and should come before any stream capture.  All calls share the
  * scratch, so calls that may overlap on the GPU (other streams, other host threads)
- * race and must be serialised by the caller. */
+ * race and must be serialised by the caller.  The resolved address is kept until
+ * the process exits: do not call this entry point after a cudaDeviceReset of that
+ * device (the scratch it would use is no longer mapped). */
 int fvm_poisson_residual_static(int ni, int nj, const double *p, const double *su, const double *ap,
                                 const double *ae, const double *aw, const double *an, const double *as,
                                 double *resid, void *stream);

@@ -14,6 +14,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
+# Builds of the same sources (oracle/Makefile): "check" is the serial checker;
+# "par" adds OpenMP to the GPU-order line sweeps and stencil loops with results
+# bit-identical to "check"; "fast" is a serial timing copy with FMA contraction.
+VARIANTS = {"check": LIB, "par": os.path.join(HERE, "_build", "liboracle_par.so"),
+            "fast": os.path.join(HERE, "_build", "liboracle_fast.so")}
+SOURCES = ("fvm_oracle.c", "fvm_oracle.h", "fvm3d_oracle.c", "fvm3d_oracle.h", "Makefile")
 
 FAITHFUL, GPU = 0, 1
 
@@ -42,22 +48,29 @@ class Post(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+def _stale(path: str) -> bool:
+    if not os.path.exists(path):
+        return True
+    t = os.path.getmtime(path)
+    return any(os.path.getmtime(os.path.join(HERE, f)) > t for f in SOURCES)
+
+
 def build(force: bool = False) -> str:
-    """Compile the restatement with its Makefile (portable flags, no FMA contraction)."""
-    src = os.path.join(HERE, "fvm_oracle.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
-        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    """Compile every variant of the restatement with its Makefile when any source,
+    header or the Makefile itself is newer than a library."""
+    if force or any(_stale(v) for v in VARIANTS.values()):
+        subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []), check=True)
     return LIB
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(variant: str = "check"):
+    """The ctypes handle of one build variant ("check", "par" or "fast")."""
+    if variant not in _libs:
         build()
-        L = ctypes.CDLL(LIB)
+        L = ctypes.CDLL(VARIANTS[variant])
         L.orc_create.restype = ctypes.c_void_p
         L.orc_create.argtypes = [ctypes.POINTER(Params)]
         L.orc_destroy.argtypes = [ctypes.c_void_p]
@@ -84,8 +97,8 @@ def lib():
         for f in ("orc_begin_step", "orc_contra_vel", "orc_explicit", "orc_iter_u", "orc_iter_v",
                   "orc_remove_grad", "orc_iter_p", "orc_correct", "orc_iter_t", "orc_calccoef"):
             getattr(L, f).argtypes = [ctypes.c_void_p]
-        _lib = L
-    return _lib
+        _libs[variant] = L
+    return _libs[variant]
 
 
 def _dptr(a: np.ndarray):
@@ -98,49 +111,50 @@ class Oracle:
 
     def __init__(self, ni, nj, re=100.0, pr=0.71, dt=0.005, vel_rot=0.0, order=GPU,
                  resimax=1e-10, nswpp=100000, thermal=True, iter_t_bug=True, res_every=1,
-                 uin=1.0, vin=0.0, tin=0.0, t_wall=1.0, dd_positional=True):
+                 uin=1.0, vin=0.0, tin=0.0, t_wall=1.0, dd_positional=True, variant="check"):
         self.ni, self.nj = ni, nj
+        self._L = lib(variant)
         p = Params(ni=ni, nj=nj, re=re, pr=pr, dt=dt, vel_rot=vel_rot, uin=uin, vin=vin, tin=tin,
                    t_wall=t_wall, resimax=resimax, nswpp=nswpp, order=order,
                    iter_t_bug=int(iter_t_bug), thermal=int(thermal), res_every=res_every,
                    dd_positional=int(dd_positional))
         self._p = p
-        self._h = lib().orc_create(ctypes.byref(p))
+        self._h = self._L.orc_create(ctypes.byref(p))
         if not self._h:
             raise ValueError("orc_create failed")
 
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
-            lib().orc_destroy(h)
+            self._L.orc_destroy(h)
             self._h = None
 
     def set_grid(self, xg, yg):
         xg = np.ascontiguousarray(xg, dtype=np.float64).ravel()
         yg = np.ascontiguousarray(yg, dtype=np.float64).ravel()
-        rc = lib().orc_set_grid(self._h, _dptr(xg), _dptr(yg))
+        rc = self._L.orc_set_grid(self._h, _dptr(xg), _dptr(yg))
         if rc != 0:
             raise ValueError(f"orc_set_grid failed ({rc})")
 
     def init(self, du=None, dv=None):
         a = None if du is None else np.ascontiguousarray(du, dtype=np.float64).ravel()
         b = None if dv is None else np.ascontiguousarray(dv, dtype=np.float64).ravel()
-        lib().orc_init(self._h, None if a is None else _dptr(a), None if b is None else _dptr(b))
+        self._L.orc_init(self._h, None if a is None else _dptr(a), None if b is None else _dptr(b))
 
     def step(self, n=1):
-        rc = lib().orc_step(self._h, n)
+        rc = self._L.orc_step(self._h, n)
         if rc != 0:
             raise FloatingPointError(f"orc_step failed ({rc})")
 
     def call(self, name):
-        return getattr(lib(), "orc_" + name)(self._h)
+        return getattr(self._L, "orc_" + name)(self._h)
 
     def set_controls(self, omega=0.0, blow=None):
         """Wall rotation rate and wall-normal blowing speeds (NJ-1 values)."""
         b = None if blow is None else np.ascontiguousarray(blow, dtype=np.float64).ravel()
         if b is not None and b.size != self.nj - 1:
             raise ValueError(f"blow needs {self.nj - 1} values")
-        lib().orc_set_controls(self._h, ctypes.c_double(omega), None if b is None else _dptr(b))
+        self._L.orc_set_controls(self._h, ctypes.c_double(omega), None if b is None else _dptr(b))
 
     STATE = ("U", "V", "P", "T", "U_N", "V_N", "T_N", "NLX", "NLY", "ADV", "NLX_NM1", "NLY_NM1", "ADV_NM1")
 
@@ -154,37 +168,37 @@ class Oracle:
         self.set_time(t)
 
     def array(self, name) -> np.ndarray:
-        p = lib().orc_array(self._h, name.encode())
+        p = self._L.orc_array(self._h, name.encode())
         if not p:
             raise KeyError(name)
         return np.ctypeslib.as_array(p, shape=(self.nj + 1, self.ni + 1))
 
     def coeffs(self) -> dict:
-        c = lib().orc_last_coeffs(self._h).contents
+        c = self._L.orc_last_coeffs(self._h).contents
         return {n: getattr(c, n) for n, _ in Coeffs._fields_}
 
     def post_begin(self):
         """POST_PROCESS with IPOST=0: time averaging from the next step on."""
-        lib().orc_post_begin(self._h)
+        self._L.orc_post_begin(self._h)
 
     def post_record(self) -> dict:
         """The POST_NU_CD_CL.PLT record of the last step."""
-        return lib().orc_post_record(self._h).contents.as_dict()
+        return self._L.orc_post_record(self._h).contents.as_dict()
 
     def post_final(self):
         """POST_PROCESS with IPOST=1: averaged coefficients and fields."""
         out = Post()
         shape = (self.nj + 1, self.ni + 1)
         f = {nm: np.zeros(shape) for nm in ("U", "V", "P", "T", "VOR")}
-        lib().orc_post_final(self._h, ctypes.byref(out), *[_dptr(f[nm]) for nm in ("U", "V", "P", "T", "VOR")])
+        self._L.orc_post_final(self._h, ctypes.byref(out), *[_dptr(f[nm]) for nm in ("U", "V", "P", "T", "VOR")])
         return out.as_dict(), f
 
     @property
     def time(self):
-        return lib().orc_time(self._h)
+        return self._L.orc_time(self._h)
 
     def set_time(self, t, niter=0):
-        lib().orc_set_time(self._h, t, niter)
+        self._L.orc_set_time(self._h, t, niter)
 
 
 # ---------------------------------------------------------------------------

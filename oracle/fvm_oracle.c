@@ -397,6 +397,7 @@ void orc_contra_vel(orc *o)
 static void nl(orc *o, const double *in, double *out)
 {
     const int NI = o->NI, NJ = o->NJ;
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= NJ - 1; j++)
         for (int i = 1; i <= NI - 1; i++) {
             int c = ID(i, j);
@@ -413,6 +414,7 @@ static void dif_diagonal(orc *o, const double *f, double *out)
 {
     const int NI = o->NI, NJ = o->NJ;
     const double *J = o->DJAC, *Q = o->Q12;
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= NJ - 1; j++)
         for (int i = 1; i <= NI - 1; i++) {
             int e = ID(i + 1, j), w = ID(i - 1, j), nn = ID(i, j + 1), s = ID(i, j - 1);
@@ -440,6 +442,7 @@ static void dif(orc *o, const double *in, double *out)
 {
     const int NI = o->NI, NJ = o->NJ;
     dif_diagonal(o, in, o->DD);
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= NJ - 1; j++)
         for (int i = 1; i <= NI - 1; i++) {
             int c = ID(i, j);
@@ -456,6 +459,7 @@ static void p_source(orc *o)
 {
     const int NI = o->NI, NJ = o->NJ;
     const double *J = o->DJAC, *P = o->P;
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= NJ - 1; j++)
         for (int i = 1; i <= NI - 1; i++) {
             int e = ID(i + 1, j), w = ID(i - 1, j), nn = ID(i, j + 1), s = ID(i, j - 1);
@@ -479,10 +483,9 @@ static inline int jwrap(const orc *o, int j)
 /* One radial line j: Thomas along i with the reference's recurrences
  * (iter_u.f90:52-64, lisolv.f90:72-84).  B(0)=0 is the reference's never-written
  * SAVE element.  jn/js are the rows read for the explicit neighbour terms. */
-static void radial_line(orc *o, double *phi, int j, int jn, int js)
+static void radial_line(orc *o, double *phi, int j, int jn, int js, double *B, double *D)
 {
     const int NI = o->NI;
-    double *B = o->lb, *D = o->ld;
     B[0] = 0.0;
     for (int i = 1; i <= NI - 1; i++) {
         int c = ID(i, j);
@@ -499,12 +502,21 @@ static void radial_line(orc *o, double *phi, int j, int jn, int js)
  * (ghost rows at the branch cut), or zebra order with periodic wrap. */
 static void sweep_radial(orc *o, double *phi)
 {
-    const int NJ = o->NJ;
+    const int NI = o->NI, NJ = o->NJ;
     if (o->p.order == ORC_FAITHFUL) {
-        for (int j = 1; j <= NJ - 1; j++) radial_line(o, phi, j, j + 1, j - 1);
+        for (int j = 1; j <= NJ - 1; j++) radial_line(o, phi, j, j + 1, j - 1, o->lb, o->ld);
     } else {
-        for (int c = 1; c >= 0; c--) /* odd lines (colour 0) first, then even lines */
-            for (int j = 2 - c; j <= NJ - 1; j += 2) radial_line(o, phi, j, jwrap(o, j + 1), jwrap(o, j - 1));
+        /* the lines of one colour are independent: any thread count gives the
+           same bits (each thread has its own recurrence scratch) */
+        for (int c = 1; c >= 0; c--) { /* odd lines (colour 0) first, then even lines */
+#pragma omp parallel
+            {
+                double B[NI + 1], D[NI + 1];
+#pragma omp for schedule(static)
+                for (int j = 2 - c; j <= NJ - 1; j += 2)
+                    radial_line(o, phi, j, jwrap(o, j + 1), jwrap(o, j - 1), B, D);
+            }
+        }
     }
 }
 
@@ -562,19 +574,24 @@ static void sweep_theta(orc *o, double *phi)
         return;
     }
     const int n = NJ - 1;
-    double *a = o->la, *b = o->lb, *cc = o->lc, *d = o->ld, *x = o->lx;
-    for (int col = 1; col >= 0; col--)
-        for (int i = 2 - col; i <= NI - 1; i += 2) {
-            for (int j = 1; j <= n; j++) {
-                int c = ID(i, j);
-                a[j] = -o->AS[c];
-                b[j] = o->AP[c];
-                cc[j] = -o->AN[c];
-                d[j] = (o->AE[c] * phi[ID(i + 1, j)] + o->AW[c] * phi[ID(i - 1, j)]) + o->SU[c];
+    for (int col = 1; col >= 0; col--) {
+#pragma omp parallel
+        {
+            double a[n + 2], b[n + 2], cc[n + 2], d[n + 2], x[n + 2], bb[n + 2], u[n + 2], z[n + 2], w[n + 2];
+#pragma omp for schedule(static)
+            for (int i = 2 - col; i <= NI - 1; i += 2) {
+                for (int j = 1; j <= n; j++) {
+                    int c = ID(i, j);
+                    a[j] = -o->AS[c];
+                    b[j] = o->AP[c];
+                    cc[j] = -o->AN[c];
+                    d[j] = (o->AE[c] * phi[ID(i + 1, j)] + o->AW[c] * phi[ID(i - 1, j)]) + o->SU[c];
+                }
+                cyclic(n, a, b, cc, d, x, bb, u, z, w);
+                for (int j = 1; j <= n; j++) phi[ID(i, j)] = x[j];
             }
-            cyclic(n, a, b, cc, d, x, o->lbb, o->lu, o->lz, o->lw);
-            for (int j = 1; j <= n; j++) phi[ID(i, j)] = x[j];
         }
+    }
 }
 
 /* ------------------------------------------------------------------------- */
@@ -585,6 +602,7 @@ static void af_coeffs(orc *o, const double *m1, const double *m2, double rek)
 {
     const int NI = o->NI, NJ = o->NJ;
     const double *J = o->DJAC;
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= NJ - 1; j++)
         for (int i = 1; i <= NI - 1; i++) {
             int c = ID(i, j), e = ID(i + 1, j), w = ID(i - 1, j), nn = ID(i, j + 1), s = ID(i, j - 1);
@@ -600,6 +618,7 @@ static void af_cross(orc *o, const double *m1, const double *m2, const double *f
 {
     const int NI = o->NI, NJ = o->NJ;
     const double *J = o->DJAC;
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= NJ - 1; j++)
         for (int i = 1; i <= NI - 1; i++) {
             int e = ID(i + 1, j), w = ID(i - 1, j), nn = ID(i, j + 1), s = ID(i, j - 1);
@@ -619,6 +638,7 @@ static void iter_af(orc *o, int kind, double *phi, const double *phin, const dou
     /* first factor: x-split coefficients (iter_u.f90:13-46) */
     af_coeffs(o, o->XIX, o->ETX, rek);
     af_cross(o, o->XIX, o->ETX, phi);
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= NJ - 1; j++)
         for (int i = 1; i <= NI - 1; i++) {
             int c = ID(i, j);
@@ -634,6 +654,7 @@ static void iter_af(orc *o, int kind, double *phi, const double *phin, const dou
     /* ITER_T builds this cross term from V (iter_T.f90:89-95) */
     const double *fx = (kind == BC_T && o->p.iter_t_bug) ? o->V : phi;
     af_cross(o, o->XIY, o->ETY, fx);
+#pragma omp parallel for schedule(static)
     for (int j = 1; j <= NJ - 1; j++)
         for (int i = 1; i <= NI - 1; i++) {
             int c = ID(i, j);
@@ -685,6 +706,7 @@ static int iter_p(orc *o)
     for (;;) {
         niter = niter + 1;
         dif_diagonal(o, o->P, o->DD);
+#pragma omp parallel for schedule(static)
         for (int j = 1; j <= NJ - 1; j++)
             for (int i = 1; i <= NI - 1; i++) {
                 int c = ID(i, j);

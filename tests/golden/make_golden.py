@@ -1,7 +1,7 @@
 """Generate the golden fixtures by running the reference's own Fortran sources.
 
-Usage (only where the reference tree exists):
-    python tests/golden/make_golden.py /root/reference [--3d-only | --program-only]
+Usage (only where the reference tree exists; its root directory is required):
+    python tests/golden/make_golden.py REFERENCE_ROOT [--3d-only | --program-only]
 
 For each case the R2D snapshot (cylinder/cylinder_v3.0.3_AF_original 4step_face_nl)
 is executed by ftn_interp with NI, NJ (and where stated NSWPP, RESIMAX) replaced in
@@ -242,7 +242,10 @@ def run_case(ref_root, c):
 
 def main():
     pos = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref_root = pos[0] if pos else "/root/reference"
+    if not pos or not os.path.isdir(pos[0]):
+        sys.exit("usage: make_golden.py REFERENCE_ROOT [--3d-only | --program-only]  "
+                 "(the root directory of the reference source tree)")
+    ref_root = pos[0]
     only3d = "--3d-only" in sys.argv
     only_prog = "--program-only" in sys.argv
     manifest = []

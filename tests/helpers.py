@@ -31,11 +31,11 @@ def make_case(n_theta=32, n_r=24, re=100.0, pr=0.71, dt=0.005, skew=0.0, amp=1e-
                 thermal=thermal, vel_rot=vel_rot)
 
 
-def make_oracle(case, order=oracle.GPU, res_every=2):
+def make_oracle(case, order=oracle.GPU, res_every=2, variant="check"):
     g = case["g"]
     o = oracle.Oracle(g.ni, g.nj, re=case["re"], pr=case["pr"], dt=case["dt"], vel_rot=case["vel_rot"],
                       order=order, resimax=case["resimax"], nswpp=case["nswpp"],
-                      thermal=case["thermal"], res_every=res_every)
+                      thermal=case["thermal"], res_every=res_every, variant=variant)
     o.set_grid(g.xg, g.yg)
     o.init(case["du"], case["dv"])
     return o

@@ -72,8 +72,45 @@ def test_static_residual_matches_the_step_residual():
     assert abs(got[1] - ref) <= 1e-12 * abs(ref), (got, ref)
 
 
-def test_static_residual_rejects_oversized_grids():
+def _numpy_residual(P, SU, AP, AE, AW, AN, AS, ni, nj):
+    """sum|r| / sum|AP*P| over the interior in float64, circumferential neighbours
+    through the periodic branch cut (the entry point's documented formula)."""
+    i = np.arange(1, ni)[None, :]
+    j = np.arange(1, nj)[:, None]
+    jn = np.where(j == nj - 1, 1, j + 1)
+    js = np.where(j == 1, nj - 1, j - 1)
+    r = ((((AE[j, i] * P[j, i + 1] + AW[j, i] * P[j, i - 1]) + AN[j, i] * P[jn, i]) + AS[j, i] * P[js, i])
+         + SU[j, i]) - AP[j, i] * P[j, i]
+    return np.abs(r).sum() / np.abs(AP[j, i] * P[j, i]).sum()
+
+
+def test_static_residual_at_the_size_limit():
+    """1024 x 1024 interior cells, the largest grid accepted: every one of the 2048
+    scratch slots and the arrival ticket behind them are in use."""
+    torch = pytest.importorskip("torch")
+    ni = nj = 1025
+    rng = np.random.default_rng(7)
+    arrays = [rng.uniform(-1.0, 1.0, size=(nj + 1, ni + 1)) for _ in range(7)]
+    arrays[2] = arrays[2] + 4.0   # AP dominant, as in the pressure equation
+    want = _numpy_residual(*arrays, ni, nj)
+    dev = [torch.tensor(a.ravel(), dtype=torch.float64, device="cuda") for a in arrays]
+    out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
     L = capi.load()
-    dummy = [ctypes.c_void_p(8)] * 8
-    assert L.fvm_poisson_residual_static(2000, 2000, *dummy, None) == capi.FVM_ERR_ARG
-    assert L.fvm_poisson_residual_static(97, 129, *([None] * 8), None) == capi.FVM_ERR_ARG
+    ptrs = [ctypes.c_void_p(a.data_ptr()) for a in dev]
+    for k in range(2):
+        rc = L.fvm_poisson_residual_static(ni, nj, *ptrs, ctypes.c_void_p(out[k:].data_ptr()), None)
+        assert rc == capi.FVM_OK
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert abs(got[0] - want) <= 1e-12 * want, (got, want)
+    assert abs(got[1] - want) <= 1e-12 * want, (got, want)
+
+
+def test_static_residual_rejects_oversized_grids():
+    # Null pointers throughout: the size check must refuse these before any
+    # pointer is used, so a broken check can never reach a kernel launch.
+    L = capi.load()
+    null = [None] * 8
+    assert L.fvm_poisson_residual_static(1025, 1026, *null, None) == capi.FVM_ERR_ARG   # one row too many
+    assert L.fvm_poisson_residual_static(2000, 2000, *null, None) == capi.FVM_ERR_ARG
+    assert L.fvm_poisson_residual_static(97, 129, *null, None) == capi.FVM_ERR_ARG
