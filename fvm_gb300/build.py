@@ -16,7 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfvm_gb300.so")
-SOURCES = ["fvm_setup.cu", "fvm_step.cu", "fvm_mixed.cu", "fvm_capi.cu", "fvm_static.cu", "fvm_batch.cu", "fvm_adjoint.cu", "fvm3d.cu", "fvm_post.cu"]
+SOURCES = ["fvm_setup.cu", "fvm_step.cu", "fvm_mixed.cu", "fvm_resident.cu", "fvm_capi.cu", "fvm_static.cu",
+           "fvm_batch.cu", "fvm_adjoint.cu", "fvm3d.cu", "fvm_post.cu"]
 HEADERS = ["fvm_internal.cuh", "fvm_ops.cuh", "fvm_df.cuh", os.path.join("..", "..", "include", "fvm.h"),
            os.path.join("..", "..", "include", "fvm3d.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -25,7 +26,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxe
 # correction sweeps of the mixed path (far-field residuals reach the subnormal range,
 # which measured slower); FP64 is unaffected, and fvm3d.cu keeps them for its
 # double-float arithmetic.
-FTZ_SOURCES = {"fvm_mixed.cu", "fvm_adjoint.cu"}
+FTZ_SOURCES = {"fvm_mixed.cu", "fvm_resident.cu", "fvm_adjoint.cu"}
 
 
 def _nvcc() -> str:

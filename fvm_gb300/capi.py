@@ -26,7 +26,8 @@ EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", 
            "fvm_set_time", "fvm_set_controls", "fvm_adjoint_drag_grad", "fvm_adjoint_vjp", "fvm_begin_step", "fvm_contra_vel", "fvm_nl", "fvm_dif", "fvm_p_source",
            "fvm_iter_u", "fvm_iter_v", "fvm_remove_grad", "fvm_iter_p", "fvm_correct", "fvm_iter_t",
            "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize", "fvm_get_stream",
-           "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps", "fvm_poisson_residual_static",
+           "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps", "fvm_resident_wait_test",
+           "fvm_poisson_residual_static",
            "fvm_batch_create", "fvm_batch_destroy", "fvm_batch_last_error", "fvm_batch_case",
            "fvm_batch_tiles", "fvm_batch_set_tiles", "fvm_batch_autotune", "fvm_batch_time_sweeps",
            "fvm_batch_step", "fvm_batch_get_timing", "fvm_post_begin", "fvm_post_get", "fvm_post_final",
@@ -44,7 +45,8 @@ class Params(ctypes.Structure):
                 ("poisson_groups", ctypes.c_int), ("poisson_host_loop", ctypes.c_int),
                 ("dd_positional", ctypes.c_int),
                 ("tile_r_warps", ctypes.c_int), ("tile_r_m", ctypes.c_int),
-                ("tile_t_warps", ctypes.c_int), ("tile_t_m", ctypes.c_int)]
+                ("tile_t_warps", ctypes.c_int), ("tile_t_m", ctypes.c_int),
+                ("poisson_resident", ctypes.c_int)]
 
 
 class Coeffs(ctypes.Structure):
@@ -132,6 +134,7 @@ def load(build_if_missing: bool = True):
     L.fvm_timing_reset.argtypes = [V]
     L.fvm_get_timing.argtypes = [V, ctypes.POINTER(Timing)]
     L.fvm_time_sweeps.argtypes = [V, ctypes.c_int, D, ctypes.POINTER(ctypes.c_longlong)]
+    L.fvm_resident_wait_test.argtypes = [V, ctypes.c_int]
     L.fvm_poisson_residual_static.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 8 + [V]
     I = ctypes.POINTER(ctypes.c_int)
     L.fvm_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(Params), ctypes.POINTER(V)]
@@ -342,6 +345,11 @@ class Context:
         self._ok(self.L.fvm_time_sweeps(self.h, sweeps, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+    def resident_wait_test(self, max_polls=4096) -> int:
+        """fvm_resident_wait_test: status code (FVM_ERR_TIMEOUT when the bounded
+        waits of the resident sweeps reported running out)."""
+        return self.L.fvm_resident_wait_test(self.h, max_polls)
+
     def timing(self) -> dict:
         t = Timing()
         self._ok(self.L.fvm_get_timing(self.h, ctypes.byref(t)))
@@ -430,6 +438,11 @@ class Batch:
         arr = (Coeffs * (n * k))()
         self._ok(self.L.fvm_batch_step(self.h, n, arr), allow=(FVM_ERR_NOCONV,))
         return [[arr[s * k + j].as_dict() for j in range(k)] for s in range(n)]
+
+    def resident_wait_test(self, max_polls=4096) -> int:
+        """fvm_resident_wait_test: status code (FVM_ERR_TIMEOUT when the bounded
+        waits of the resident sweeps reported running out)."""
+        return self.L.fvm_resident_wait_test(self.h, max_polls)
 
     def timing(self) -> dict:
         t = Timing()

@@ -45,6 +45,10 @@ int check_params(const fvm_params *p, std::string &why)
     };
     if (!tile_ok(p->tile_r_warps, p->tile_r_m, p->ni - 1, "radial")) return FVM_ERR_ARG;
     if (!tile_ok(p->tile_t_warps, p->tile_t_m, p->nj - 1, "circumferential")) return FVM_ERR_ARG;
+    if (p->poisson_resident < 0 || (p->poisson_resident >= 2 && p->poisson_resident % 2)) {
+        why = "poisson_resident: 0, 1 or an even number of lines per block";
+        return FVM_ERR_ARG;
+    }
     return FVM_OK;
 }
 
@@ -78,6 +82,7 @@ int fvm_default_params(fvm_params *p)
     p->poisson_groups = 16;
     p->poisson_host_loop = 1;
     p->dd_positional = 1;
+    p->poisson_resident = 1;
     return FVM_OK;
 }
 
@@ -104,6 +109,7 @@ int fvm_create(const fvm_params *p, fvm_ctx **out)
         return FVM_ERR_CUDA;
     }
     int rc = fvm::setup_allocate(c);
+    if (rc == FVM_OK) rc = fvm::resident_setup(c);
     if (rc != FVM_OK) {
         fvm_destroy(c);
         return rc;
@@ -317,6 +323,13 @@ int fvm_get_timing(fvm_ctx *c, fvm_timing *out)
     if (!c || !out) return FVM_ERR_ARG;
     *out = c->tm;
     return FVM_OK;
+}
+
+int fvm_resident_wait_test(fvm_ctx *c, int max_polls)
+{
+    READY();
+    if (max_polls < 1 || max_polls > (1 << 24)) return bad(c, "max_polls must be in 1 .. 2^24");
+    return fvm::run_resident_wait_test(c, max_polls);
 }
 
 }  // extern "C"

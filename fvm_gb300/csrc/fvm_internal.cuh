@@ -49,7 +49,7 @@ struct PCtl {
     int niter;          // sweeps done in the current ITER_P
     int done;           // 1 once converged or capped
     int capped;         // 1 if stopped at the cap above tolerance
-    int pad;
+    int fault;          // 1 if a bounded wait of the resident sweep kernel ran out
     double resip;       // last scaled residual
     unsigned int ticket;
     unsigned int pad2;
@@ -102,6 +102,10 @@ struct Dev {
     double *SU, *SUV, *SUT, *DD;   // per-field right-hand sides (U uses SU)
     // mixed-precision scratch
     float *RF, *DF;                // FP32 residual right-hand side and correction
+    // line-resident sweeps: boundary-line exchange words (value bits | tag << 32),
+    // [slot 0/1][line][element], and each block's count of completed sweeps
+    unsigned long long *XW;
+    unsigned int *XCNT;
     double *W64;                   // FP64 scratch line values (defect correction)
     // reductions
     PCtl *pctl;
@@ -164,6 +168,10 @@ struct fvm_ctx {
     bool capturing = false;
     fvm_timing tm{};
     fvm_adj *adj = nullptr;
+    // line-resident Poisson sweeps (mixed path): lines per block (0: per-colour
+    // launches), blocks, and whether the launch carries the cooperative attribute
+    int res_lines = 0, res_blocks = 0;
+    bool res_coop = false;
     fvm::PostState post;
     int post_suspend = 0;   // recomputation passes of the adjoint: no post-processing
 };
@@ -244,6 +252,7 @@ double *post_array(fvm_ctx *c, const char *name);
 int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out);
 double *array_by_name(fvm_ctx *c, const char *name);
 int run_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launches);
+int run_resident_wait_test(fvm_ctx *c, int max_polls);
 // launch sequences shared by single contexts and batches (fvm_step.cu)
 int step_before_poisson(const Tgt &t);
 int poisson_bodies(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond, int groups);
@@ -261,6 +270,11 @@ int mixed_poisson_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_co
 int mixed_sweep_pair(const Tgt &t, int apply);
 int mixed_predictor_radial(const Tgt &t, int field, int colour, int refresh);
 int mixed_predictor_theta(const Tgt &t, int field, int colour, int ghosts);
+// line-resident FP32 sweeps (fvm_resident.cu)
+int resident_setup(fvm_ctx *c);
+int resident_sweeps(const Tgt &t, int sweeps, int apply, int max_polls, unsigned tag_skew,
+                    cudaGraphConditionalHandle cond, int has_cond, int check_done);
+int resident_reset(fvm_ctx *c);
 }  // namespace fvm
 
 // ---------------------------------------------------------------------------------
@@ -321,30 +335,70 @@ __device__ __forceinline__ void gsync()
     else __syncwarp();
 }
 
+// Barrier of one line group: the whole block (the group is the block, or every
+// group of the block runs the same barrier sequence) ...
+template <int NW>
+struct BlockSync {
+    __device__ __forceinline__ void operator()() const { gsync<NW>(); }
+};
+// ... or the group's own named barrier (id >= 1, the group's 32*NW threads), so that
+// groups of one block synchronise independently.
+template <int NW>
+struct NamedSync {
+    int id;
+    __device__ __forceinline__ void operator()() const
+    {
+        if (NW > 1) asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(WARP * NW) : "memory");
+        else __syncwarp();
+    }
+};
+
 __device__ __forceinline__ int spad(int e) { return e + (e >> 5); }
 
-template <typename T, int M, int NW>
-__device__ __forceinline__ void to_chunks(T (&v)[M], T *sm, int t)
+// Rounded operations whose order the compiler cannot change.  An expression with
+// two products and a sum may be contracted either way; these fix the form, so that
+// every kernel computing the same quantity gives the same bits.
+// (other arithmetic types, e.g. double-float pairs: their own operators, a*b then + c)
+template <typename T>
+__device__ __forceinline__ T fma_rn(T a, T b, T c) { return a * b + c; }
+template <typename T>
+__device__ __forceinline__ T mul_rn(T a, T b) { return a * b; }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
+// Right-hand side of a line of the FP32 Poisson correction sweep:
+// (AN x(j+1) + AS x(j-1)) + r, in one fixed rounding order.
+__device__ __forceinline__ float pois32_rhs(float an, float xn, float as, float xs, float r)
+{
+    return add_rn(fma_rn(an, xn, mul_rn(as, xs)), r);
+}
+
+template <typename T, int M, int NW, class Sync = BlockSync<NW>>
+__device__ __forceinline__ void to_chunks(T (&v)[M], T *sm, int t, Sync sync = Sync())
 {
     constexpr int TG = WARP * NW;
 #pragma unroll
     for (int k = 0; k < M; k++) sm[spad(k * TG + t)] = v[k];
-    gsync<NW>();
+    sync();
 #pragma unroll
     for (int k = 0; k < M; k++) v[k] = sm[spad(t * M + k)];
-    gsync<NW>();
+    sync();
 }
 
-template <typename T, int M, int NW>
-__device__ __forceinline__ void to_interleaved(T (&v)[M], T *sm, int t)
+template <typename T, int M, int NW, class Sync = BlockSync<NW>>
+__device__ __forceinline__ void to_interleaved(T (&v)[M], T *sm, int t, Sync sync = Sync())
 {
     constexpr int TG = WARP * NW;
 #pragma unroll
     for (int k = 0; k < M; k++) sm[spad(t * M + k)] = v[k];
-    gsync<NW>();
+    sync();
 #pragma unroll
     for (int k = 0; k < M; k++) v[k] = sm[spad(k * TG + t)];
-    gsync<NW>();
+    sync();
 }
 
 // Apply the precomputed LU factors of one line to the right-hand side held in
@@ -354,9 +408,9 @@ __device__ __forceinline__ void to_interleaved(T (&v)[M], T *sm, int t)
 // Each first-order recurrence runs sequentially inside a chunk, the chunks are
 // combined by a Kogge-Stone scan of affine maps across the warp and by a short
 // fold across the group's warps (xch: 2*NW values of shared scratch), then fixed up.
-template <typename T, int M, int NW>
+template <typename T, int M, int NW, class Sync = BlockSync<NW>>
 __device__ __forceinline__ void group_apply_r(T (&v)[M], const T (&fi)[M], const T (&fa)[M], const T (&fb)[M], int t,
-                                              T *xch)
+                                              T *xch, Sync sync = Sync())
 {
     const int lane = t & (WARP - 1), wl = t / WARP;
     T gk[M];
@@ -364,7 +418,7 @@ __device__ __forceinline__ void group_apply_r(T (&v)[M], const T (&fi)[M], const
 #pragma unroll
     for (int k = 0; k < M; k++) {
         T a = fa[k];
-        y = a * y + fi[k] * v[k];
+        y = fma_rn(a, y, mul_rn(fi[k], v[k]));
         v[k] = y;
         g = g * a;
         gk[k] = g;
@@ -378,9 +432,9 @@ __device__ __forceinline__ void group_apply_r(T (&v)[M], const T (&fi)[M], const
     T yw = T(0);
     if (NW > 1) {
         if (lane == WARP - 1) { xch[2 * wl] = G; xch[2 * wl + 1] = Y; }
-        __syncthreads();
+        sync();
         for (int w2 = 0; w2 < wl; w2++) yw = xch[2 * w2 + 1] + xch[2 * w2] * yw;
-        __syncthreads();
+        sync();
     }
     {
         T Yp = shfl_up(Y, 1), Gp = shfl_up(G, 1);
@@ -406,9 +460,9 @@ __device__ __forceinline__ void group_apply_r(T (&v)[M], const T (&fi)[M], const
     T xw = T(0);
     if (NW > 1) {
         if (lane == 0) { xch[2 * wl] = H; xch[2 * wl + 1] = X; }
-        __syncthreads();
+        sync();
         for (int w2 = NW - 1; w2 > wl; w2--) xw = xch[2 * w2 + 1] + xch[2 * w2] * xw;
-        __syncthreads();
+        sync();
     }
     {
         T Xn = shfl_down(X, 1), Hn = shfl_down(H, 1);

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(128) k_pois32(const __grid_constant__ S src, i
         v[k] = 0.0f;
         if (active && e < n) {
             int i = e + 1;
-            v[k] = (an[k] * d.DF[IDX(i, jn)] + as[k] * d.DF[IDX(i, js)]) + d.RF[IDX(i, j)];
+            v[k] = pois32_rhs(an[k], d.DF[IDX(i, jn)], as[k], d.DF[IDX(i, js)], d.RF[IDX(i, j)]);
         }
     }
     if (stop) return;
@@ -158,6 +158,10 @@ static int sweep_pair(const Tgt &t, int apply, int check_done)
 
 int mixed_sweep_pair(const Tgt &t, int apply) { return sweep_pair(t, apply, 0); }
 
+// One FP32 correction sweep of the per-colour path on the current state, whatever
+// path the context's step uses (tests compare the two paths).
+int mixed_sweep_percolour(const Tgt &t, int apply) { return sweep_pair(t, apply, 0); }
+
 // One outer iteration of the MIXED Poisson: FP64 residual (ends the device-side
 // loop when converged or capped), then refine_sweeps FP32 zebra sweeps, the last
 // of which adds the correction to P.
@@ -170,6 +174,8 @@ int mixed_poisson_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_co
     });
     KCOUNT(t.c);
     FVM_LAUNCH_CHECK(t.c);
+    if (!t.tab.devs && t.c->res_lines)   // one context: the interval in one resident launch
+        return resident_sweeps(t, t.refine_sweeps, 1, 0, 0u, cond, has_cond, 1);
     for (int s = 0; s < t.refine_sweeps; s++) {
         int rc = sweep_pair(t, s == t.refine_sweeps - 1, 1);
         if (rc) return rc;

@@ -1,0 +1,324 @@
+// fvm_resident.cu -- line-resident zebra sweeps of the FP32 Poisson correction
+// (mixed precision): one launch runs a whole refinement interval.
+//
+// The per-colour path launches one grid per zebra colour (two per sweep), and each
+// launch re-reads its line factors, couplings and right-hand side from L2.  Here
+// the radial lines j = 1..NJ-1 are split into blocks of B consecutive lines (B
+// even); each CTA keeps its lines' FP32 factors, couplings, right-hand side and
+// current correction on chip (registers and shared memory) for all refine_sweeps
+// sweeps of the interval, so a sweep moves nothing but the boundary lines between
+// neighbouring CTAs.
+//
+// Zebra order (odd lines, then even lines; lisolv.f90:18-33 reordered as in the
+// per-colour kernels, neighbours through the periodic branch cut).  A CTA owning
+// lines j0 .. j0+B-1 (j0 odd) also solves line j0+B, the first (odd) line of the
+// next CTA, redundantly in the odd half: its even line j0+B-1 then finds both
+// neighbours on chip, and the only data from other CTAs a sweep needs are the
+// previous sweep's values of line j0-1 (last line of the CTA before) and of line
+// j0+B+1 (second line of the CTA after).  One exchange per sweep, both directions
+// at once.  The redundant line's result is bit-identical to its owner's (same
+// inputs, same code).
+//
+// Exchange without flags or fences: every published element is one 64-bit word
+// (FP32 value bits | tag << 32) written and polled with relaxed gpu-scope 64-bit
+// accesses (single-copy atomic), so a word whose tag matches carries the value of
+// that sweep.  Tags are the CTA's count of completed sweeps (kept in XCNT across
+// launches, equal in every CTA), words alternate between two slots by sweep
+// parity, and a slot is overwritten only after both readers have passed the sweep
+// that read it.  Every wait is bounded (max_polls); a wait that runs out sets the
+// control block's fault flag, ends the Poisson loop and returns, and the host
+// reports FVM_ERR_TIMEOUT and clears the exchange state.
+//
+// The arithmetic of a line (right-hand side, precomputed-factor solve, correction
+// added to P in FP64 with the BCP ghosts refreshed) is the per-colour kernel's,
+// operation for operation, so both paths give identical bits.  Compiled with
+// -ftz=true, as the per-colour sweeps are.
+#include <type_traits>
+
+#include "fvm_internal.cuh"
+#include "fvm_ops.cuh"
+
+namespace fvm {
+namespace {
+
+__device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_word(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Shared memory of a block: the block's current line values (B+1 lines, LW words
+// each) and one fold buffer per line group.  Every value of the block stays in the
+// chunk ownership of the line solve (thread t of a group holds elements
+// t*M .. t*M+M-1); a line is stored as word k*TG + t = element t*M + k, so a
+// neighbouring group reads exactly the elements its own thread t needs, bank-
+// conflict free, and no transpose is needed.
+template <int M, int NW>
+struct ResLayout {
+    // block size bound: wide chunks (M >= 6) keep their values in up to 128
+    // registers per thread, so their blocks stay within 512 threads
+    static constexpr int MAXT = M >= 6 ? 512 : 1024;
+    static constexpr int TG = WARP * NW;
+    static constexpr int LW = TG * M;   // words per line
+    static size_t bytes(int B) { return sizeof(float) * size_t(B + 1) * (LW + 2 * NW); }
+    // largest block of this instantiation (the dynamic shared memory allowed for it)
+    static size_t max_bytes() { return bytes(MAXT / TG - 1); }
+};
+
+// Lines j0 .. j0+B-1 of block blockIdx.x and the redundant line j0+B: group g
+// (32*NW threads) owns line j0+g.  S sweeps; apply != 0 adds the correction to P
+// afterwards.  check_done != 0 returns at once when the loop is already done.
+template <int M, int NW, int HAS_COND>
+__global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
+    k_pois32_resident(const __grid_constant__ Dev d, int B, int S, int apply, int check_done, int max_polls,
+                      unsigned tag_skew, cudaGraphConditionalHandle cond)
+{
+    using Lay = ResLayout<M, NW>;
+    constexpr int TG = Lay::TG, LW = Lay::LW;
+    extern __shared__ float shm[];
+    __shared__ int s_fault, s_stop;
+    float *lines = shm;
+    const int g = threadIdx.x / TG, t = threadIdx.x % TG;
+    float *xch = shm + size_t(B + 1) * LW + size_t(g) * 2 * NW;
+    const NamedSync<NW> bar{1 + g};
+    const int L = d.NJ - 1;
+    const int j0 = blockIdx.x * B + 1;
+    auto wrap = [L](int j) { return j < 1 ? j + L : (j > L ? j - L : j); };
+    const int j = wrap(j0 + g);
+    const int n = d.sP.n;
+    if (threadIdx.x == 0) {   // the loop's done flag, read once for the whole block
+        s_fault = 0;
+        s_stop = check_done ? d.pctl->done : 0;
+    }
+    __syncthreads();
+    if (s_stop) return;
+
+    const LineSys &s = d.sP;
+    const size_t base = size_t(j - 1) * LW;
+    float fi[M], fa[M], fb[M], an[M], as[M], rf[M], v[M], halo[M];
+    load_factors<float, M, NW>(fi, fa, fb, s.invDf + base, s.faf + base, s.fbf + base, t);
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        const int e = t * M + k;   // chunk ownership
+        const bool ok = e < n;
+        const int c = IDX(e + 1, j);
+        an[k] = ok ? d.cP.ANf[c] : 0.0f;
+        as[k] = ok ? d.cP.ASf[c] : 0.0f;
+        rf[k] = ok ? d.RF[c] : 0.0f;
+        halo[k] = 0.0f;   // the correction starts from zero
+        v[k] = 0.0f;
+        lines[g * LW + k * TG + t] = 0.0f;
+    }
+    const unsigned cnt0 = d.XCNT[blockIdx.x];
+    const bool odd_line = (g & 1) == 0;            // j0 is odd: even g = colour 0
+    const bool publish = g == 1 || g == B - 1;     // read by the blocks before / after
+    const int hline = g == 0 ? wrap(j0 - 1) : (g == B ? wrap(j0 + B + 1) : 0);
+    __syncthreads();
+
+    int sw = 1;
+    for (; sw <= S; sw++) {
+        // odd lines (and the redundant first line of the next block)
+        if (odd_line) {
+            if (sw > 1 && hline) {
+                const unsigned want = cnt0 + unsigned(sw - 1) + tag_skew;
+                const unsigned long long *src = d.XW + (size_t((sw - 1) & 1) * L + (hline - 1)) * LW;
+                unsigned pending = 0;
+#pragma unroll
+                for (int k = 0; k < M; k++)
+                    if (t * M + k < n) pending |= 1u << k;
+                for (int it = 0; pending && it < max_polls; it++) {
+#pragma unroll
+                    for (int k = 0; k < M; k++) {
+                        if (!((pending >> k) & 1u)) continue;
+                        const unsigned long long w = ld_word(src + k * TG + t);
+                        if (unsigned(w >> 32) == want) {
+                            halo[k] = __uint_as_float(unsigned(w));
+                            pending &= ~(1u << k);
+                        }
+                    }
+                }
+                if (pending) s_fault = 1;
+            }
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const float xs = g == 0 ? halo[k] : lines[(g - 1) * LW + k * TG + t];
+                const float xn = g == B ? halo[k] : lines[(g + 1) * LW + k * TG + t];
+                v[k] = t * M + k < n ? pois32_rhs(an[k], xn, as[k], xs, rf[k]) : 0.0f;
+            }
+            group_apply_r<float, M, NW>(v, fi, fa, fb, t, xch, bar);
+#pragma unroll
+            for (int k = 0; k < M; k++) lines[g * LW + k * TG + t] = v[k];
+        }
+        __syncthreads();
+        if (s_fault) break;   // read by every thread after the barrier: a uniform exit
+        // even lines: both neighbours are on chip
+        if (!odd_line) {
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const float xs = lines[(g - 1) * LW + k * TG + t];
+                const float xn = lines[(g + 1) * LW + k * TG + t];
+                v[k] = t * M + k < n ? pois32_rhs(an[k], xn, as[k], xs, rf[k]) : 0.0f;
+            }
+            group_apply_r<float, M, NW>(v, fi, fa, fb, t, xch, bar);
+#pragma unroll
+            for (int k = 0; k < M; k++) lines[g * LW + k * TG + t] = v[k];
+            if (publish) {
+                unsigned long long *dst = d.XW + (size_t(sw & 1) * L + (j - 1)) * LW;
+                const unsigned long long tag = (unsigned long long)(cnt0 + unsigned(sw)) << 32;
+#pragma unroll
+                for (int k = 0; k < M; k++)
+                    if (t * M + k < n) st_word(dst + k * TG + t, tag | __float_as_uint(v[k]));
+            }
+        }
+        __syncthreads();
+    }
+
+    if (sw <= S) {   // a wait ran out: end the loop, leave P alone
+        if (threadIdx.x == 0) {
+            d.pctl->fault = 1;
+            d.pctl->done = 1;
+            if (HAS_COND) cudaGraphSetConditional(cond, 0);
+        }
+        return;
+    }
+    if (g < B) {
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            const int e = t * M + k;
+            if (e < n) d.DF[IDX(e + 1, j)] = v[k];
+        }
+        if (apply) {
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const int e = t * M + k;
+                if (e < n) d.P[IDX(e + 1, j)] += (double)v[k];
+            }
+            bar();
+            if (t < WARP) refresh_row_ghosts<BCK_POISSON>(d, d.P, d.P, j, nullptr, nullptr, t);
+        }
+    }
+    if (threadIdx.x == 0) d.XCNT[blockIdx.x] = cnt0 + unsigned(S);
+}
+
+template <int M, int NW, int HAS_COND>
+cudaError_t launch_resident(const fvm_ctx *c, cudaStream_t st, int S, int apply, int check_done, int max_polls,
+                            unsigned skew, cudaGraphConditionalHandle cond)
+{
+    using Lay = ResLayout<M, NW>;
+    auto k = k_pois32_resident<M, NW, HAS_COND>;
+    const size_t smem = Lay::bytes(c->res_lines);   // allowed by resident_setup
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c->res_blocks);
+    cfg.blockDim = dim3((c->res_lines + 1) * Lay::TG);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = c->res_coop ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, c->d, c->res_lines, S, apply, check_done, max_polls, skew, cond);
+}
+
+}  // namespace
+
+// Bounded wait of one exchange: about 1 s of polling at L2 latency.
+constexpr int kResidentPolls = 1 << 21;
+
+// Lines per block for the context (0: the per-colour path).  poisson_resident = 1
+// takes 4 lines per block where they fit (measured fastest on 512 x 384: 2.40 us
+// per sweep against 2.57 with 2), else the smallest even B dividing NJ-1 whose
+// blocks are all co-resident; k >= 2 asks for k lines per block.
+int resident_setup(fvm_ctx *c)
+{
+    c->res_lines = c->res_blocks = 0;
+    c->res_coop = false;
+    const int want = c->p.poisson_resident;
+    if (c->p.precision != FVM_MIXED || want == 0) return FVM_OK;
+    const LineSys &s = c->d.sP;
+    const int L = c->NJ - 1, TG = WARP * s.NW;
+    int sms = 0;
+    FVM_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->p.device));
+    const int order[] = {4, 2, 6, 8, 10, 12, 14};
+    for (int B : order) {
+        if (want >= 2 && B != want) continue;
+        if (L % B || L / B < 2) continue;
+        int per_sm = 0;
+        cudaError_t e = cudaSuccess;
+        bool ok = dispatch_line(s, [&](auto m, auto nw) {
+            constexpr int M_ = decltype(m)::value, NW_ = decltype(nw)::value;
+            if ((B + 1) * TG > ResLayout<M_, NW_>::MAXT) {
+                e = cudaErrorInvalidConfiguration;
+                return;
+            }
+            auto k0 = k_pois32_resident<M_, NW_, 0>;
+            auto k1 = k_pois32_resident<M_, NW_, 1>;
+            const size_t smem = ResLayout<M_, NW_>::bytes(B);
+            // both variants may use the shared memory of their largest block (set here,
+            // outside any stream capture; the same value for every context)
+            const int cap = (int)ResLayout<M_, NW_>::max_bytes();
+            e = cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k1, (B + 1) * TG, smem);
+        });
+        if (!ok || e != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (L / B <= per_sm * sms) {
+            c->res_lines = B;
+            c->res_blocks = L / B;
+            c->res_coop = true;
+            break;
+        }
+    }
+    if (want >= 2 && !c->res_lines) {
+        c->err = "poisson_resident: the requested lines per block do not divide NJ-1 into co-resident blocks";
+        return FVM_ERR_ARG;
+    }
+    return FVM_OK;
+}
+
+// One launch of the resident sweeps for a single context (batches use the
+// per-colour path).  max_polls <= 0 takes the default bound.
+int resident_sweeps(const Tgt &t, int sweeps, int apply, int max_polls, unsigned tag_skew,
+                    cudaGraphConditionalHandle cond, int has_cond, int check_done)
+{
+    fvm_ctx *c = t.c;
+    cudaError_t e = cudaErrorInvalidValue;
+    const int polls = max_polls > 0 ? max_polls : kResidentPolls;
+    bool ok = dispatch_line(c->d.sP, [&](auto m, auto nw) {
+        constexpr int M_ = decltype(m)::value, NW_ = decltype(nw)::value;
+        if (has_cond) e = launch_resident<M_, NW_, 1>(c, t.st, sweeps, apply, check_done, polls, tag_skew, cond);
+        else e = launch_resident<M_, NW_, 0>(c, t.st, sweeps, apply, check_done, polls, tag_skew, cond);
+    });
+    if (!ok) {
+        c->err = "line length above 512 cells is not supported";
+        return FVM_ERR_ARG;
+    }
+    if (e != cudaSuccess) {
+        c->err = std::string("resident sweep launch: ") + cudaGetErrorString(e);
+        return FVM_ERR_CUDA;
+    }
+    KCOUNT(c);
+    return FVM_OK;
+}
+
+// After a wait ran out: the blocks' sweep counts may disagree, so clear the
+// exchange words, the counts and the fault flag (stream-ordered).
+int resident_reset(fvm_ctx *c)
+{
+    const size_t words = 2 * size_t(c->NJ - 1) * WARP * 4 * 4;
+    FVM_CUDA(c, cudaMemsetAsync(c->d.XW, 0, words * sizeof(unsigned long long), c->stream));
+    FVM_CUDA(c, cudaMemsetAsync(c->d.XCNT, 0, size_t(c->NJ) * sizeof(unsigned int), c->stream));
+    FVM_CUDA(c, cudaMemsetAsync(&c->d.pctl->fault, 0, sizeof(int), c->stream));
+    return FVM_OK;
+}
+
+}  // namespace fvm

@@ -87,6 +87,9 @@ void carve(Bump &b, fvm_ctx *c, int nblk)
     for (auto p : st) *p = b.take<double>(n);
     d.RF = b.take<float>(n);
     d.DF = b.take<float>(n);
+    // exchange words for the largest tile (32 x 4 warps x 4 elements per line)
+    d.XW = b.take<unsigned long long>(2 * size_t(c->NJ - 1) * WARP * 4 * 4);
+    d.XCNT = b.take<unsigned int>(size_t(c->NJ));
     d.pctl = b.take<PCtl>(1);
     d.partial = b.take<double>(2 * size_t(nblk));
     d.coefrow = b.take<double>(8 * size_t(nj1));

@@ -567,7 +567,8 @@ __global__ void k_calc_final(const __grid_constant__ S src, double rtime, fvm_co
     out->cl = pl + tl;
     out->nu = -nu / d.scal[0];
     out->sweeps = d.pctl->niter;
-    out->resid = d.pctl->resip;
+    // a negative residual reports that a bounded wait of the resident sweeps ran out
+    out->resid = d.pctl->fault ? -1.0 : d.pctl->resip;
     *d.cflbits = 0ull;
 }
 
@@ -757,6 +758,8 @@ int step_after_poisson(const Tgt &t, double rtime, fvm_coeffs *dout)
 // MIXED: the FP32 correction without applying it), for timing.
 int sweep_pairs(const Tgt &t, int sweeps)
 {
+    if (t.mixed && !t.tab.devs && t.c->res_lines)   // all sweeps in one resident launch
+        return resident_sweeps(t, sweeps, 0, 0, 0u, 0, 0, 0);
     for (int s = 0; s < sweeps; s++) {
         if (t.mixed) RC(mixed_sweep_pair(t, 0));
         else {
@@ -850,9 +853,26 @@ namespace {
 // on the device without host synchronisation.  Host loop (default): the same body
 // as a plain graph, replayed by the host until the control block reports
 // completion (profilers can then see each kernel).
+int poisson_graph_build(fvm_ctx *c);
+
+// The resident sweep launch carries the cooperative attribute (all blocks
+// co-resident); if the graph cannot hold it, the graph is built again without the
+// attribute (the blocks then fit by the occupancy check of resident_setup, and
+// every wait is bounded either way).
 int poisson_graph(fvm_ctx *c)
 {
     if (c->pgraph) return FVM_OK;
+    int rc = poisson_graph_build(c);
+    if (rc == FVM_ERR_CUDA && c->res_lines && c->res_coop) {
+        cudaGetLastError();
+        c->res_coop = false;
+        rc = poisson_graph_build(c);
+    }
+    return rc;
+}
+
+int poisson_graph_build(fvm_ctx *c)
+{
     Tgt t = tgt_of(c);
     const int per = t.mixed ? t.refine_sweeps : t.res_every;
     int groups = c->p.poisson_groups > 0 ? c->p.poisson_groups : (32 + per - 1) / per;
@@ -980,10 +1000,11 @@ int time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *launch
     float ms = 0.f;
     FVM_CUDA(c, cudaEventElapsedTime(&ms, c->ev_a, c->ev_b));
     cudaGraphExecDestroy(ge);
-    *launches = 2LL * sweeps;
-    *ms_per_launch = ms / (2.0 * sweeps);
+    const bool resident = c->p.precision == FVM_MIXED && c->res_lines;
+    *launches = resident ? 1LL : 2LL * sweeps;
+    *ms_per_launch = ms / (2.0 * sweeps);   // per zebra colour
     c->tm.sweep_span_ms += ms;
-    c->tm.sweep_span_launches += 2LL * sweeps;
+    c->tm.sweep_span_launches += *launches;
     return FVM_OK;
 }
 
@@ -999,6 +1020,16 @@ int calccoef_copy(fvm_ctx *c, fvm_coeffs *dout, fvm_coeffs *out)
     return FVM_OK;
 }
 
+// A bounded wait of the resident sweeps ran out: clear the exchange state so the
+// context stays usable, and report it.
+int resident_fault(fvm_ctx *c)
+{
+    RC(resident_reset(c));
+    FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->err = "resident Poisson sweeps: a bounded wait for a neighbouring block ran out";
+    return FVM_ERR_TIMEOUT;
+}
+
 fvm_coeffs *coef_slot(fvm_ctx *c)
 {
     static_assert(sizeof(fvm_coeffs) <= 12 * sizeof(double), "coeff scratch");
@@ -1012,6 +1043,24 @@ int run_time_sweeps(fvm_ctx *c, int sweeps, double *ms_per_launch, long long *la
     return time_sweeps(c, sweeps, ms_per_launch, launches);
 }
 
+// Two resident sweeps on scratch with exchange tags no block publishes: every
+// wait at the second sweep runs out after max_polls polls.
+int run_resident_wait_test(fvm_ctx *c, int max_polls)
+{
+    if (c->p.precision != FVM_MIXED || !c->res_lines) {
+        c->err = "the context does not use the resident sweep path";
+        return FVM_ERR_ARG;
+    }
+    RC(resident_sweeps(tgt_of(c), 2, 0, max_polls, 0x40000000u, 0, 0, 0));
+    FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, c->d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
+    FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (!c->h_pctl->fault) {
+        c->err = "a wait that cannot be satisfied did not report";
+        return FVM_ERR_CUDA;
+    }
+    return resident_fault(c);
+}
+
 int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
 {
     Tgt t = tgt_of(c);
@@ -1022,6 +1071,7 @@ int run_iter_p(fvm_ctx *c, double *resid, int *sweeps)
     FVM_CUDA(c, cudaStreamSynchronize(c->stream));
     c->tm.kernel_launches += poisson_loop_kernels(c, c->h_pctl->niter);
     c->tm.sweeps += c->h_pctl->niter;
+    if (c->h_pctl->fault) return resident_fault(c);
     int status = c->h_pctl->capped ? FVM_ERR_NOCONV : FVM_OK;
     if (!std::isfinite(c->h_pctl->resip)) {
         c->err = "non-finite Poisson residual";
@@ -1076,6 +1126,7 @@ int run_step(fvm_ctx *c, int nsteps, fvm_coeffs *out)
         const double cl_prev = c->last.cl;   // CL_NM1 (calccoef.f90:109)
         fvm_coeffs co;
         RC(calccoef_copy(c, dout, &co));
+        if (co.resid < 0.0) return resident_fault(c);
         RC(post_after_calccoef(c, cl_prev, co));
         c->tm.kernel_launches += poisson_loop_kernels(c, co.sweeps);
         c->tm.sweeps += co.sweeps;

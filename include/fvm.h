@@ -71,6 +71,11 @@ typedef struct fvm_params {
        lines (NJ-1 unknowns: second factor); 32 * warps * elements must cover the
        line.  Set both of a family or neither. */
     int tile_r_warps, tile_r_m, tile_t_warps, tile_t_m;
+    /* MIXED, single context: FP32 correction sweeps of one refinement interval in
+       one launch whose blocks keep their lines on chip and exchange only boundary
+       lines (1, the default: lines per block chosen automatically; k >= 2, even:
+       k lines per block; 0: one launch per zebra colour).  Same results bit for bit. */
+    int poisson_resident;
 } fvm_params;
 
 /* Per-step diagnostics of CALCCOEF (calccoef.f90:9-120) plus Poisson statistics. */
@@ -207,8 +212,18 @@ int fvm_timing_reset(struct fvm_ctx *ctx);
 int fvm_get_timing(struct fvm_ctx *ctx, fvm_timing *out);
 /* Replays `sweeps` zebra sweeps of the Poisson sweep kernels of the context's
  * precision (touching only scratch arrays, the state is unchanged) in a graph
- * bracketed by CUDA events on the context's stream: average time per launch. */
+ * bracketed by CUDA events on the context's stream.  ms_per_launch: average time
+ * per zebra colour (the per-colour path launches once per colour; the resident
+ * path runs all sweeps in one launch, reported as 1 in *launches, and the figure
+ * is its time divided by 2*sweeps). */
 int fvm_time_sweeps(struct fvm_ctx *ctx, int sweeps, double *ms_per_launch, long long *launches);
+/* Check of the bounded waits of the resident sweeps (MIXED contexts using them):
+ * two sweeps on scratch arrays with exchange tags that no block publishes, so
+ * every wait for a neighbouring block runs out after max_polls polls (1 .. 2^24).
+ * Returns FVM_ERR_TIMEOUT when the kernel reported it, as a step would; the
+ * state is unchanged and the exchange state cleared, so the context stays usable.
+ * FVM_ERR_ARG if the context does not use the resident path. */
+int fvm_resident_wait_test(struct fvm_ctx *ctx, int max_polls);
 
 /* Allocation-free scaled residual of the pressure equation.  No counterpart in
  * the reference: it serves callers that cannot allocate device memory (code
