@@ -229,6 +229,7 @@ inline void with_src(const Tgt &t, F &&f)
 
 Tgt tgt_of(fvm_ctx *c);
 int setup_allocate(fvm_ctx *c);
+void radial_tile(const fvm_ctx *c, int &nw, int &m);
 int setup_factors(fvm_ctx *c);
 int setup_controls(fvm_ctx *c, double omega, const double *blow);
 int setup_grid(fvm_ctx *c);

@@ -41,10 +41,12 @@
 namespace fvm {
 namespace {
 
+// volatile: re-executed on every poll; no memory clobber, so the loads of one poll
+// can all be in flight at once
 __device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p)
 {
     unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p));
     return v;
 }
 
@@ -133,12 +135,15 @@ __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
                 for (int k = 0; k < M; k++)
                     if (t * M + k < n) pending |= 1u << k;
                 for (int it = 0; pending && it < max_polls; it++) {
+                    // one L2 round trip per poll: every pending word's load is issued
+                    // before any is tested
+                    unsigned long long w[M];
+#pragma unroll
+                    for (int k = 0; k < M; k++) w[k] = ((pending >> k) & 1u) ? ld_word(src + k * TG + t) : 0ull;
 #pragma unroll
                     for (int k = 0; k < M; k++) {
-                        if (!((pending >> k) & 1u)) continue;
-                        const unsigned long long w = ld_word(src + k * TG + t);
-                        if (unsigned(w >> 32) == want) {
-                            halo[k] = __uint_as_float(unsigned(w));
+                        if (((pending >> k) & 1u) && unsigned(w[k] >> 32) == want) {
+                            halo[k] = __uint_as_float(unsigned(w[k]));
                             pending &= ~(1u << k);
                         }
                     }

@@ -18,11 +18,20 @@ from tests.helpers import make_case, make_gpu
 
 pytestmark = pytest.mark.gpu
 
+def resident_auto_tile(n_r):
+    """The radial tile a MIXED context with resident sweeps picks when none is given:
+    one warp up to 128 cells, else two-warp groups with the fewest elements per
+    thread that cover the line."""
+    if n_r <= 128:
+        return (1, -(-n_r // 32))
+    return (2, next(m for m in (1, 2, 3, 4, 6, 8) if 64 * m >= n_r))
+
+
 CASES = [
-    # n_theta, n_r, lines per block (1 = automatic), radial tile (0, 0 = automatic)
-    (512, 384, 1, (0, 0)),     # the benchmark grid, automatic choice
-    (512, 384, 4, (0, 0)),
-    (128, 96, 2, (0, 0)),      # the 128 x 96 grid
+    # n_theta, n_r, lines per block (1 = automatic), radial tile
+    (512, 384, 1, resident_auto_tile(384)),   # the benchmark grid, automatic choices
+    (512, 384, 4, (4, 3)),
+    (128, 96, 2, resident_auto_tile(96)),     # the 128 x 96 grid
     (128, 96, 4, (0, 0)),
     (96, 300, 6, (2, 6)),      # two-warp groups of 6 elements per thread
     (64, 380, 2, (1, 12)),     # one-warp groups of 12
@@ -53,11 +62,21 @@ def test_resident_sweeps_are_bit_identical(n_theta, n_r, lines, tile, host_loop)
         assert np.array_equal(fa[nm], fb[nm]), nm
 
 
+def test_automatic_tile_of_resident_contexts():
+    """Left automatic, a resident MIXED context takes resident_auto_tile: its steps
+    equal those of a context given that tile explicitly."""
+    case = make_case(96, 300, re=200.0, dt=0.002, resimax=1e-14, nswpp=32)
+    ra, fa = _run(case, 1, (0, 0), 1, steps=1)
+    rb, fb = _run(case, 1, resident_auto_tile(300), 1, steps=1)
+    for nm in ("U", "V", "P", "T"):
+        assert np.array_equal(fa[nm], fb[nm]), nm
+
+
 def test_resident_sweeps_converge_like_the_per_colour_path():
     """With the tolerance as the stopping rule: same sweep counts and fields."""
     case = make_case(64, 48, re=100.0, dt=0.005, skew=0.2, resimax=1e-11, nswpp=200000)
-    ra, fa = _run(case, 1, (0, 0), 1, steps=2)
-    rb, fb = _run(case, 0, (0, 0), 1, steps=2)
+    ra, fa = _run(case, 1, resident_auto_tile(48), 1, steps=2)
+    rb, fb = _run(case, 0, resident_auto_tile(48), 1, steps=2)
     assert [r["sweeps"] for r in ra] == [r["sweeps"] for r in rb]
     assert all(r["resid"] <= 1e-11 for r in ra)
     for nm in ("U", "V", "P", "T"):
