@@ -624,9 +624,11 @@ def run_les3d_bench(args):
     ctx = make_ctx3(w, capi.MIXED, local, g, du, dv, dw)
     ext = torch.cuda.ExternalStream(ctx.stream_handle())
     ctx.step(args.warmup)
-    host = {nm: torch.empty(ctx.shape, dtype=torch.float64, pin_memory=True).numpy() for nm in FIELDS3D}
-    for nm in FIELDS3D:
-        host[nm][...] = ctx.get(nm)
+    # pinned host buffers handed straight to fvm3_upload_state / fvm3_download_state
+    # (one DMA per array, one synchronisation per call)
+    host = [torch.empty(ctx.n, dtype=torch.float64, pin_memory=True) for _ in FIELDS3D]
+    ptrs = [h.data_ptr() for h in host]
+    ctx.download_ptrs(ptrs)
     e2e_ms = 0.0
     dist.barrier()
     for _ in range(args.steps):
@@ -635,11 +637,9 @@ def run_les3d_bench(args):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(ext)
-        for nm in FIELDS3D:
-            ctx.set(nm, host[nm])
+        ctx.upload_ptrs(ptrs)
         ctx.step(1)
-        for nm in FIELDS3D:
-            host[nm][...] = ctx.get(nm)
+        ctx.download_ptrs(ptrs)
         b.record(ext)
         b.synchronize()
         e2e_ms += a.elapsed_time(b)
@@ -777,6 +777,117 @@ def run_sweep_bench(args):
 
 
 # ---------------------------------------------------------------------------------
+# acceptance on the 128 x 96 Re=100 case: mean Cd, rms Cl and St of the FP64 and the
+# mixed path over whole shedding periods from the same developed state
+# ---------------------------------------------------------------------------------
+ACCEPT = dict(name="acceptance-cylinder2d-re100-128x96", n_theta=128, n_r=96, re=100.0, pr=0.71, dt=0.005,
+              resimax=1e-10, nswpp=1000000, amp=1e-3, seed=0, dr1=0.005, r_out=50.0, res_every=8,
+              refine_sweeps=32)
+
+
+def shedding_stats(hist):
+    """Mean Cd, rms Cl (about its mean) and the Strouhal number from the upward zero
+    crossings of Cl - mean(Cl) (linear interpolation in time; D = U = 1) over a
+    record list."""
+    import numpy as np
+    t = np.array([h["time"] for h in hist])
+    cd = np.array([h["cd"] for h in hist])
+    cl = np.array([h["cl"] for h in hist])
+    c = cl - cl.mean()
+    up = np.nonzero((c[:-1] < 0.0) & (c[1:] >= 0.0))[0]
+    tc = t[up] + (t[up + 1] - t[up]) * (-c[up]) / (c[up + 1] - c[up])
+    st = (len(tc) - 1) / (tc[-1] - tc[0]) if len(tc) >= 2 else float("nan")
+    return {"cd_mean": float(cd.mean()), "cl_rms": float(np.sqrt(np.mean(c * c))), "st": float(st),
+            "cl_amp": float(0.5 * (cl.max() - cl.min())), "periods": int(max(len(tc) - 1, 0))}
+
+
+def run_acceptance(args):
+    import numpy as np
+    import torch
+    from fvm_gb300 import capi, dist
+    rank, world = dist.init("nccl")
+    local = dist.rank_world()[2]
+    torch.cuda.set_device(local)
+    a = dict(ACCEPT)
+    g, du, dv = case_inputs(a)
+
+    def make(precision):
+        p = capi.default_params(ni=g.ni, nj=g.nj, re=a["re"], pr=a["pr"], dt=a["dt"], resimax=a["resimax"],
+                                nswpp=a["nswpp"], thermal=0, precision=precision, res_every=a["res_every"],
+                                refine_sweeps=a["refine_sweeps"], adi_refine=2, device=local, poisson_host_loop=0)
+        ctx = capi.Context(p)
+        ctx.set_grid(g.xg, g.yg)
+        return ctx
+
+    # spin-up (mixed path) from the seeded start, one shedding period (~1212 steps) per
+    # chunk, until the lift amplitude of two consecutive chunks agrees to 1 % (or the
+    # time limit); the lift amplitudes of the chunks are reported
+    per = 1212
+    ctx = make(capi.MIXED)
+    ctx.init(du, dv)
+    amps, t0, sweeps = [], time.perf_counter(), []
+    while True:
+        ctx.step(per)
+        h = ctx.history(per)
+        cl = np.array([r["cl"] for r in h])
+        amps.append(float(0.5 * (cl.max() - cl.min())))
+        sweeps.append(float(np.mean([r["sweeps"] for r in h])))
+        tnow = h[-1]["time"]
+        print(f"acceptance spin-up: t={tnow:.1f} cl_amp={amps[-1]:.4f} sweeps/step={sweeps[-1]:.0f} "
+              f"{time.perf_counter() - t0:.0f} s", file=sys.stderr, flush=True)
+        if (tnow >= args.spinup_min and len(amps) >= 2 and amps[-1] > 0.05
+                and abs(amps[-1] - amps[-2]) <= 0.01 * amps[-1]) or tnow >= args.spinup_max:
+            break
+    spin_s = time.perf_counter() - t0
+    state = ctx.download(("U", "V", "P", "T", "NLX", "NLY", "ADV"))
+    t_start = h[-1]["time"]
+    ctx.close()
+
+    # the window: the same number of steps from the same state in each precision
+    steps = int(round(args.window_periods * per))
+    res = {}
+    for name, prec in (("mixed", capi.MIXED), ("fp64", capi.FP64)):
+        c = make(prec)
+        c.upload(state["U"], state["V"], state["P"], state["T"], state["NLX"], state["NLY"], state["ADV"])
+        c.set_time(t_start)
+        c.post_begin()
+        clk = ClockSampler(local)
+        clk.start()
+        hist, t1, done = [], time.perf_counter(), 0
+        while done < steps:
+            n = min(1000, steps - done)
+            c.step(n)
+            hist += c.history(n)
+            done += n
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t1
+        clocks = clk.stop()
+        post = c.post_get()
+        st = shedding_stats(hist)
+        res[name] = dict(st, post_record={k: post[k] for k in ("cd", "rms_cl", "st", "st_last", "cl_amp", "niter")},
+                         sweeps_per_step=float(np.mean([r["sweeps"] for r in hist])),
+                         max_resid=float(max(r["resid"] for r in hist)), ms_per_step=1e3 * wall / steps,
+                         clocks=clocks)
+        print(f"acceptance {name}: {wall:.0f} s, {json.dumps(st)}", file=sys.stderr, flush=True)
+        c.close()
+    rel = {k: abs(res["mixed"][k] - res["fp64"][k]) / abs(res["fp64"][k]) for k in ("cd_mean", "cl_rms", "st")}
+    out = {"metric": "mean Cd, rms Cl, St: mixed vs FP64 GPU (bar 0.1 %)", "workload": a["name"],
+           "config": {"grid": "128 theta x 96 r", "re": a["re"], "dt": a["dt"],
+                      "poisson": f"scaled-L1 {a['resimax']:g} (no sweep cap in effect)",
+                      "start": f"seeded {a['amp']:g} perturbation, spin-up on the mixed path until the lift "
+                               f"amplitude of two consecutive {per}-step chunks agreed to 1 %",
+                      "spinup": {"t_end": t_start, "chunk_cl_amp": amps, "sweeps_per_step": sweeps,
+                                 "seconds": spin_s},
+                      "window": {"steps": steps, "t": [t_start, t_start + steps * a["dt"]],
+                                 "from": "the same downloaded state (U, V, P, NLX, NLY) in both precisions"}},
+           "fp64": res["fp64"], "mixed": res["mixed"], "mixed_vs_fp64_rel": rel,
+           "within_0.1_percent": bool(all(v <= 1e-3 for v in rel.values()))}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    dist.finalize()
+
+
+# ---------------------------------------------------------------------------------
 # reference arm
 # ---------------------------------------------------------------------------------
 def run_reference(args):
@@ -859,11 +970,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--parts", choices=["all", "mixed", "fp64"], default="all",
                     help="'mixed' / 'fp64' time one precision only (profiler runs; fp64: les3d only)")
-    ap.add_argument("--workload", choices=["cylinder2d", "sweep64", "adjoint", "les3d"], default="cylinder2d",
+    ap.add_argument("--workload", choices=["cylinder2d", "sweep64", "adjoint", "les3d", "acceptance"],
+                    default="cylinder2d",
                     help="sweep64: 64 ragged cases advanced as batches, sharded over the ranks; "
                          "adjoint: window-drag gradient on the 128x96 grid; "
                          "les3d: 3-D LES on the 256x192x48 grid, FP64 and mixed")
     ap.add_argument("--spinup", type=int, default=200, help="adjoint workload: steps before the window")
+    ap.add_argument("--spinup-min", type=float, default=100.0, help="acceptance: earliest end of the spin-up (time)")
+    ap.add_argument("--spinup-max", type=float, default=300.0, help="acceptance: latest end of the spin-up (time)")
+    ap.add_argument("--window-periods", type=float, default=5.0,
+                    help="acceptance: window length in shedding periods of ~1212 steps")
     ap.add_argument("--poisson-loop", choices=["device", "host"], default="device",
                     help="cylinder2d and les3d: the Poisson loop on the device (graph while node) or replayed by "
                          "the host (kernels listed by ncu)")
@@ -881,6 +997,8 @@ def main():
         run_adjoint_bench(args)
     elif args.workload == "les3d":
         run_les3d_bench(args)
+    elif args.workload == "acceptance":
+        run_acceptance(args)
     else:
         run_ours(args)
 

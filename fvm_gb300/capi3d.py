@@ -11,7 +11,8 @@ from . import capi
 ROUTINES = ["fvm3_begin_step", "fvm3_contra_vel", "fvm3_nl", "fvm3_stress_tensor", "fvm3_dif", "fvm3_p_source",
             "fvm3_remove_grad", "fvm3_correct", "fvm3_iter_t"]
 EXPORTS = ["fvm3_default_params", "fvm3_create", "fvm3_destroy", "fvm3_last_error", "fvm3_set_grid", "fvm3_init",
-           "fvm3_step", "fvm3_get_array", "fvm3_set_array", "fvm3_sgs", "fvm3_time_sweeps", "fvm3_get_stream",
+           "fvm3_step", "fvm3_get_array", "fvm3_set_array", "fvm3_upload_state", "fvm3_download_state",
+           "fvm3_sgs", "fvm3_time_sweeps", "fvm3_get_stream",
            "fvm3_iter_u", "fvm3_iter_p", "fvm3_calccoef", "fvm3_test_filter", "fvm3_post_begin", "fvm3_post_get",
            "fvm3_post_steps", "fvm3_post_end"] + ROUTINES
 
@@ -54,6 +55,8 @@ def load():
         L.fvm3_step.argtypes = [V, ctypes.c_int, ctypes.POINTER(Coeffs3)]
         L.fvm3_get_array.argtypes = [V, ctypes.c_char_p, D]
         L.fvm3_set_array.argtypes = [V, ctypes.c_char_p, D]
+        L.fvm3_upload_state.argtypes = [V] + [D] * 9
+        L.fvm3_download_state.argtypes = [V] + [D] * 9
         L.fvm3_sgs.argtypes = [V, ctypes.POINTER(Coeffs3)]
         L.fvm3_time_sweeps.argtypes = [V, ctypes.c_int, D]
         L.fvm3_get_stream.argtypes = [V, ctypes.POINTER(V)]
@@ -197,6 +200,29 @@ class Context3:
         out = np.empty(self.n)
         self._ok(self.L.fvm3_get_array(self.h, name.encode(), _dp(out)))
         return out.reshape(self.shape)
+
+    STATE = ("U", "V", "W", "P", "T", "NLX", "NLY", "NLZ", "ADV")
+
+    def upload_ptrs(self, ptrs):
+        """fvm3_upload_state from nine raw host addresses in STATE order (0 skips an
+        array); page-locked buffers make each copy one DMA transfer."""
+        P = ctypes.POINTER(ctypes.c_double)
+        self._ok(self.L.fvm3_upload_state(self.h, *[ctypes.cast(p, P) if p else None for p in ptrs]))
+
+    def download_ptrs(self, ptrs):
+        P = ctypes.POINTER(ctypes.c_double)
+        self._ok(self.L.fvm3_download_state(self.h, *[ctypes.cast(p, P) if p else None for p in ptrs]))
+
+    def upload(self, **arrays):
+        """fvm3_upload_state from numpy arrays named as in STATE (missing: skipped)."""
+        arrs = [None if arrays.get(nm) is None else self._arr(arrays[nm]) for nm in self.STATE]
+        self._ok(self.L.fvm3_upload_state(self.h, *[None if a is None else _dp(a) for a in arrs]))
+
+    def download(self, names=STATE) -> dict:
+        """fvm3_download_state into fresh arrays shaped like the state."""
+        out = {nm: np.empty(self.shape) for nm in names}
+        self._ok(self.L.fvm3_download_state(self.h, *[_dp(out[nm]) if nm in out else None for nm in self.STATE]))
+        return out
 
     def set(self, name, a):
         a = self._arr(a)

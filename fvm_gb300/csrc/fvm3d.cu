@@ -2716,6 +2716,41 @@ int fvm3_set_array(fvm3_ctx *c, const char *name, const double *in)
     return FVM_OK;
 }
 
+int fvm3_upload_state(fvm3_ctx *c, const double *u, const double *v, const double *w, const double *p,
+                      const double *t, const double *nlx, const double *nly, const double *nlz, const double *adv)
+{
+    if (!c) return FVM_ERR_ARG;
+    if (!c->grid_set) return f3::bad3(c, "fvm3_set_grid has not been called");
+    const size_t bytes = sizeof(double) * c->n;
+    f3::D3 &d = c->d;
+    const double *src[] = {u, v, w, p, t, nlx, nly, nlz, adv};
+    double *dst[] = {d.U, d.V, d.W, d.P, d.T, d.NLX, d.NLY, d.NLZ, d.ADV};
+    std::vector<double *> shadowed;
+    for (int k = 0; k < 9; k++) {
+        if (!src[k]) continue;
+        F3CUDA(c, cudaMemcpyAsync(dst[k], src[k], bytes, cudaMemcpyHostToDevice, c->stream));
+        if (c->d.dfl && dst[k] >= c->shadow_lo && dst[k] < c->shadow_hi) shadowed.push_back(dst[k]);
+    }
+    if (!shadowed.empty()) F3RC(f3::refresh(c, shadowed));   // double-float shadows (mixed path)
+    F3CUDA(c, cudaStreamSynchronize(c->stream));
+    c->init_done = true;
+    return FVM_OK;
+}
+
+int fvm3_download_state(fvm3_ctx *c, double *u, double *v, double *w, double *p, double *t, double *nlx,
+                        double *nly, double *nlz, double *adv)
+{
+    if (!c) return FVM_ERR_ARG;
+    const size_t bytes = sizeof(double) * c->n;
+    f3::D3 &d = c->d;
+    double *dst[] = {u, v, w, p, t, nlx, nly, nlz, adv};
+    const double *src[] = {d.U, d.V, d.W, d.P, d.T, d.NLX, d.NLY, d.NLZ, d.ADV};
+    for (int k = 0; k < 9; k++)
+        if (dst[k]) F3CUDA(c, cudaMemcpyAsync(dst[k], src[k], bytes, cudaMemcpyDeviceToHost, c->stream));
+    F3CUDA(c, cudaStreamSynchronize(c->stream));
+    return FVM_OK;
+}
+
 int fvm3_sgs(fvm3_ctx *c, fvm3_coeffs *out)
 {
     if (!c) return FVM_ERR_ARG;

@@ -121,9 +121,22 @@ int fvm3_post_begin(struct fvm3_ctx *ctx);
 int fvm3_post_get(struct fvm3_ctx *ctx, const char *name, double *out);
 int fvm3_post_steps(struct fvm3_ctx *ctx, int *steps);
 int fvm3_post_end(struct fvm3_ctx *ctx);
-/* Named arrays ("U","V","W","P","T","NLX","NLY","NLZ","ADV","DJAC","SGS_X",...). */
+/* Named arrays ("U","V","W","P","T","NLX","NLY","NLZ","ADV","DJAC","SGS_X",...).
+ * One array per call, synchronised before returning. */
 int fvm3_get_array(struct fvm3_ctx *ctx, const char *name, double *out);
 int fvm3_set_array(struct fvm3_ctx *ctx, const char *name, const double *in);
+/* Host <-> device copies of the whole time-step state: the RESTART000.DAT contents
+ * (RLES/writedata.f90:191-215, read back as RLES/init.f90:183-205) -- U, V, W, P, T
+ * and the advection history NLX, NLY, NLZ, ADV, each (NI+1)*(NJ+1)*(NK+1) doubles in
+ * the array layout above.  Any pointer may be NULL to skip that array.  One
+ * asynchronous copy per array on the context's stream and a single synchronisation
+ * per call; page-locked host buffers (cudaHostAlloc, cudaHostRegister) make each
+ * copy one DMA transfer.  Upload requires fvm3_set_grid and stands in for
+ * fvm3_init (a restart). */
+int fvm3_upload_state(struct fvm3_ctx *ctx, const double *u, const double *v, const double *w, const double *p,
+                      const double *t, const double *nlx, const double *nly, const double *nlz, const double *adv);
+int fvm3_download_state(struct fvm3_ctx *ctx, double *u, double *v, double *w, double *p, double *t,
+                        double *nlx, double *nly, double *nlz, double *adv);
 /* One application of the SGS model (STRESS_TENSOR_DY) to the current state, for
  * tests of the model alone. */
 int fvm3_sgs(struct fvm3_ctx *ctx, fvm3_coeffs *out);

@@ -216,3 +216,39 @@ def test_device_poisson_loop_equals_host_loop(precision):
     assert out[0][0] == out[1][0]
     for nm in ("U", "V", "W", "P", "T"):
         assert np.array_equal(out[0][1][nm], out[1][1][nm]), nm
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.MIXED], ids=["fp64", "mixed"])
+def test_bulk_state_round_trip(precision):
+    """fvm3_download_state / fvm3_upload_state carry the whole time-step state (the
+    RESTART000.DAT arrays): a context restored from them continues exactly as the
+    original, and the bulk download equals the per-array reads."""
+    g = o_grid_3d(16, 12, 8, lz=np.pi, dr1=0.01, skew=0.3)
+    du, dv, dw = perturbation_3d(g.ni, g.nj, g.nk, 0.05, 3)
+
+    def make():
+        p = capi3d.default_params(ni=g.ni, nj=g.nj, nk=g.nk, re=3900.0, dt=0.002, resimax=1e-9, nswpp=400,
+                                  use_les=1, thermal=1, res_every=2, ref_a=np.pi, precision=precision,
+                                  refine_sweeps=8)
+        ctx = capi3d.Context3(p)
+        ctx.set_grid(g)
+        return ctx
+
+    a = make()
+    a.init(du, dv, dw)
+    a.step(2)
+    state = a.download()
+    for nm in capi3d.Context3.STATE:
+        assert np.array_equal(state[nm], a.get(nm)), nm
+    b = make()
+    b.upload(**state)
+    ca, cb = a.step(2), b.step(2)
+    assert ca["cd"] == cb["cd"] and ca["sweeps"] == cb["sweeps"]
+    for nm in capi3d.Context3.STATE:
+        assert np.array_equal(a.get(nm), b.get(nm)), nm
+    # pinned host buffers through the raw-pointer form
+    torch = pytest.importorskip("torch")
+    host = [torch.empty(a.n, dtype=torch.float64, pin_memory=True) for _ in capi3d.Context3.STATE]
+    a.download_ptrs([h.data_ptr() for h in host])
+    for h, nm in zip(host, capi3d.Context3.STATE):
+        assert np.array_equal(h.numpy().reshape(a.shape), a.get(nm)), nm
