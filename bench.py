@@ -238,6 +238,20 @@ def roofline_sweep(w, ms_per_colour, peaks, mixed, resident=False):
     return out
 
 
+def fp64_pipe(profile, kernel):
+    """FP64-pipe figures of an FP64 kernel from a committed ncu summary
+    (profiles/<profile>.json): the pipe's busy fraction of the active cycles — how
+    close the kernel runs to GB300's FP64 issue rate — and FP64 instructions per
+    active cell.  None when the summary is absent."""
+    path = os.path.join(ROOT, "profiles", profile + ".json")
+    try:
+        k = json.load(open(path))["kernels"][kernel]
+    except Exception:
+        return None
+    return {"pipe_busy_frac": k["fp64_pipe_busy_pct"] / 100.0, "fp64_instr_per_cell": k.get("fp64_instr_per_cell"),
+            "source": f"profiles/{profile}.json (ncu, sm__pipe_fp64_cycles_active)"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -256,7 +270,8 @@ def run_ours(args):
         peaks = json.load(open(pk))
 
     res = {}
-    parts = (("mixed", capi.MIXED),) if args.parts == "mixed" else (("mixed", capi.MIXED), ("fp64", capi.FP64))
+    parts = {"all": (("mixed", capi.MIXED), ("fp64", capi.FP64)), "mixed": (("mixed", capi.MIXED),),
+             "fp64": (("fp64", capi.FP64),)}[args.parts]
     for name, prec in parts:
         ctx = make_ctx(w, prec, local, g, du, dv)
         ext = torch.cuda.ExternalStream(ctx.stream_handle())
@@ -282,10 +297,11 @@ def run_ours(args):
                          sweep_ms=sweep_ms, resident=(sweep_launches == 1))
         ctx.close()
 
-    if args.parts == "mixed":   # profiling runs: the headline path only
+    if args.parts != "all":   # profiling runs: one path only
+        nm = parts[0][0]
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "parts": "mixed", "ms_per_step": res["mixed"]["ms"] / args.steps,
-                              "sweep_us": res["mixed"]["sweep_ms"] * 1e3}), flush=True)
+            print(json.dumps({"metric": METRIC, "parts": nm, "ms_per_step": res[nm]["ms"] / args.steps,
+                              "sweep_us": res[nm]["sweep_ms"] * 1e3}), flush=True)
         dist.finalize()
         return
     # e2e through the C-ABI with host buffers (mixed path)
@@ -324,6 +340,8 @@ def run_ours(args):
     e2e_value = units / (e2e_ms * 1e-3) / 1e6
     roof = roofline_sweep(w, res["mixed"]["sweep_ms"], peaks, True, res["mixed"]["resident"])
     roof64 = roofline_sweep(w, res["fp64"]["sweep_ms"], peaks, False)
+    if roof64:
+        roof64["fp64_issue"] = fp64_pipe("fp64_pipe_cylinder2d_512x384", "k_pois64")
     traffic_file = os.path.join(ROOT, "profiles", ("k_pois32_resident_cylinder2d_512x384.json"
                                                    if res["mixed"]["resident"] else
                                                    "k_pois32_cylinder2d_512x384.json"))
@@ -386,7 +404,7 @@ ADJOINT = dict(name="adjoint-cylinder2d-re100-128x96", n_theta=128, n_r=96, re=1
                omega=0.0, blow_sigma=0.01)
 
 
-def adjoint_measure(spinup, precision, device, fd_check=True):
+def adjoint_measure(spinup, precision, device, fd_check=True, window=None, ckpt=None, fd_blow=0):
     """Spin-up, then the window forward alone and the adjoint call (its own
     forward pass, the recomputation of every segment and the reverse pass), both
     timed; the rotation gradient is compared with a central difference (h=1e-6) of
@@ -395,6 +413,10 @@ def adjoint_measure(spinup, precision, device, fd_check=True):
     import torch
     from fvm_gb300 import capi
     a = dict(ADJOINT)
+    if window:
+        a["window"] = window
+    if ckpt:
+        a["ckpt"] = ckpt
     g, du, dv = case_inputs(a)
     p = capi.default_params(ni=g.ni, nj=g.nj, re=a["re"], pr=a["pr"], dt=a["dt"], resimax=a["resimax"],
                             nswpp=a["nswpp"], thermal=0, precision=precision, res_every=8, refine_sweeps=16,
@@ -413,9 +435,9 @@ def adjoint_measure(spinup, precision, device, fd_check=True):
     def restore():
         ctx.upload(start["U"], start["V"], start["P"], start["T"], start["NLX"], start["NLY"], start["ADV"])
 
-    def window_cd(omega):
+    def window_cd(omega, b=None):
         restore()
-        ctx.set_controls(omega, blow)
+        ctx.set_controls(omega, blow if b is None else b)
         ctx.step(a["window"])
         return float(np.mean([h["cd"] for h in ctx.history(a["window"])]))
 
@@ -439,6 +461,21 @@ def adjoint_measure(spinup, precision, device, fd_check=True):
         fd = (window_cd(a["omega"] + h) - window_cd(a["omega"] - h)) / (2 * h)
         out["fd_dJ_domega"] = fd
         out["rel_err_vs_fd"] = abs(dw - fd) / abs(fd)
+    if fd_blow:
+        # central differences of the same solver for the blowing speeds with the
+        # largest gradients
+        h = 1e-6
+        ks = [int(k) for k in np.argsort(-np.abs(db))[:fd_blow]]
+        errs = []
+        for k in ks:
+            bp, bm = blow.copy(), blow.copy()
+            bp[k] += h
+            bm[k] -= h
+            fdk = (window_cd(a["omega"], bp) - window_cd(a["omega"], bm)) / (2 * h)
+            errs.append({"j": k + 1, "adjoint": float(db[k]), "fd": fdk, "rel_err": abs(db[k] - fdk) / abs(fdk)})
+        out["fd_dJ_dblow"] = errs
+    out["window"] = a["window"]
+    out["checkpoint_every"] = a["ckpt"]
     ctx.close()
     return out
 
@@ -449,8 +486,9 @@ def run_adjoint_bench(args):
     rank, world = dist.init("nccl")
     local = dist.rank_world()[2]
     torch.cuda.set_device(local)
-    res = {nm: adjoint_measure(args.spinup, prec, local) for nm, prec in (("fp64", capi.FP64), ("mixed", capi.MIXED))}
-    a = ADJOINT
+    res = {nm: adjoint_measure(args.spinup, prec, local, window=args.window, ckpt=args.ckpt, fd_blow=args.fd_blow)
+           for nm, prec in (("fp64", capi.FP64), ("mixed", capi.MIXED))}
+    a = dict(ADJOINT, window=res["fp64"]["window"], ckpt=res["fp64"]["checkpoint_every"])
     out = {"metric": METRIC, "workload": a["name"], "value": res["fp64"]["adjoint_over_forward"],
            "unit": "adjoint/forward time", "n_gpus": world, "higher_is_better": False, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -675,7 +713,9 @@ def run_les3d_bench(args):
                    "l2": "256 MiB buffer written between timed steps (outside the events)"},
         "fp64": {"value": fp64_value, "ms_per_step": res["fp64"]["ms"] / args.steps,
                  "sweeps_per_step": res["fp64"]["sweeps"],
-                 "roofline": roofline_sweep3d(n_int, res["fp64"]["sweep_ms"] / 2, peaks, False)},
+                 "roofline": dict(roofline_sweep3d(n_int, res["fp64"]["sweep_ms"] / 2, peaks, False) or {},
+                                  fp64_issue=fp64_pipe("fp64_pipe_les3d_192x160x32", "k3_line"),
+                                  fp64_issue_residual=fp64_pipe("fp64_pipe_les3d_192x160x32", "k3_mres"))},
         "mixed_vs_fp64": {"speedup": value / fp64_value,
                           "field_rel_l2": {nm: rel(res["mixed"]["fields"][nm], res["fp64"]["fields"][nm])
                                            for nm in ("U", "V", "W", "P", "T")},
@@ -755,6 +795,28 @@ def run_sweep_bench(args):
             ctx.close()
         one = {"value": sum(s.cells for s in mine) * 2 / t_one / 1e6, "unit": "Mcell-steps/s",
                "note": "same cases as independent contexts stepped one after another, 2 steps each"}
+    # bit-identity of the batch with the same cases run one by one over the same
+    # warm-up + timed steps (the first check_cases cases of this rank, the batch's tiles)
+    check = None
+    if args.check_cases > 0:
+        tiles = b.tiles()
+        tk = dict(tile_r_warps=tiles[0], tile_r_m=tiles[1], tile_t_warps=tiles[2], tile_t_m=tiles[3])
+        nst = args.warmup + args.steps
+        same, cases = True, []
+        for k, s in enumerate(mine[:args.check_cases]):
+            want = {nm: b.cases[k].get(nm) for nm in ("U", "V", "P")}
+            ctx = capi.Context(batch.case_params(s, capi.MIXED, **kw, **tk))
+            g, du, dv = batch.case_inputs(s)
+            ctx.set_grid(g.xg, g.yg)
+            ctx.init(du, dv)
+            ctx.step(nst)
+            eq = all(np.array_equal(ctx.get(nm), want[nm]) for nm in want)
+            same = same and eq
+            cases.append({"n_theta": s.n_theta, "n_r": s.n_r, "re": s.re, "bit_identical": eq})
+            ctx.close()
+        check = {"steps": nst, "cases": cases, "all_bit_identical": same,
+                 "note": "the batch's fields after all its steps against the same cases stepped one by one "
+                         "with the batch's tiles"}
     b.close()
     out = {"metric": METRIC, "workload": sw["name"], "value": value, "unit": "Mcell-steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt_max / args.steps,
@@ -770,7 +832,7 @@ def run_sweep_bench(args):
                       "partition": [len(p) for p in parts],
                       "setup_s_rank": setup_s,
                       "l2": "inputs larger than L2 (about 0.5 GB of case state)"},
-           "one_by_one": one, "gpu_launches": int(launches), "clocks": clocks}
+           "one_by_one": one, "batch_vs_one_by_one": check, "gpu_launches": int(launches), "clocks": clocks}
     if rank == 0:
         print(json.dumps(out), flush=True)
     dist.finalize()
@@ -969,13 +1031,19 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--parts", choices=["all", "mixed", "fp64"], default="all",
-                    help="'mixed' / 'fp64' time one precision only (profiler runs; fp64: les3d only)")
+                    help="'mixed' / 'fp64' time one precision only (profiler runs)")
     ap.add_argument("--workload", choices=["cylinder2d", "sweep64", "adjoint", "les3d", "acceptance"],
                     default="cylinder2d",
                     help="sweep64: 64 ragged cases advanced as batches, sharded over the ranks; "
                          "adjoint: window-drag gradient on the 128x96 grid; "
                          "les3d: 3-D LES on the 256x192x48 grid, FP64 and mixed")
     ap.add_argument("--spinup", type=int, default=200, help="adjoint workload: steps before the window")
+    ap.add_argument("--window", type=int, default=0, help="adjoint: drag-averaging window in steps (0: 100)")
+    ap.add_argument("--ckpt", type=int, default=0, help="adjoint: checkpoint interval in steps (0: 10)")
+    ap.add_argument("--fd-blow", type=int, default=0,
+                    help="adjoint: also check this many blowing components against central differences")
+    ap.add_argument("--check-cases", type=int, default=0,
+                    help="sweep64: compare this many cases with one-by-one runs of the same steps, bit for bit")
     ap.add_argument("--spinup-min", type=float, default=100.0, help="acceptance: earliest end of the spin-up (time)")
     ap.add_argument("--spinup-max", type=float, default=300.0, help="acceptance: latest end of the spin-up (time)")
     ap.add_argument("--window-periods", type=float, default=5.0,
