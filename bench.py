@@ -342,6 +342,7 @@ def run_ours(args):
     roof64 = roofline_sweep(w, res["fp64"]["sweep_ms"], peaks, False)
     if roof64:
         roof64["fp64_issue"] = fp64_pipe("fp64_pipe_cylinder2d_512x384", "k_pois64")
+        roof64["fp64_issue_residual"] = fp64_pipe("fp64_pipe_cylinder2d_512x384", "k_pres64")
     traffic_file = os.path.join(ROOT, "profiles", ("k_pois32_resident_cylinder2d_512x384.json"
                                                    if res["mixed"]["resident"] else
                                                    "k_pois32_cylinder2d_512x384.json"))
@@ -715,7 +716,7 @@ def run_les3d_bench(args):
                  "sweeps_per_step": res["fp64"]["sweeps"],
                  "roofline": dict(roofline_sweep3d(n_int, res["fp64"]["sweep_ms"] / 2, peaks, False) or {},
                                   fp64_issue=fp64_pipe("fp64_pipe_les3d_192x160x32", "k3_line"),
-                                  fp64_issue_residual=fp64_pipe("fp64_pipe_les3d_192x160x32", "k3_mres"))},
+                                  fp64_issue_residual=fp64_pipe("fp64_pipe_les3d_192x160x32", "k3_pres"))},
         "mixed_vs_fp64": {"speedup": value / fp64_value,
                           "field_rel_l2": {nm: rel(res["mixed"]["fields"][nm], res["fp64"]["fields"][nm])
                                            for nm in ("U", "V", "W", "P", "T")},
