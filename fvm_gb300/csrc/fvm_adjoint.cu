@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(256) k_adj_pres(Dev d, Adj a, int per, double 
             pa += fabs(cf.AP[c] * mu[c]);
         }
     }
-    if (!grid_sum2(da, ra, pa, sh, last)) return;
+    if (!grid_sum2(da, ra, pa, sh, last, d.nblk_res)) return;
     if (threadIdx.x == 0) {
         const int it = a.pctl->niter + per;
         const double resip = pa > 0.0 ? ra / pa : 0.0;
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(256) k_adj_mres(Dev d, Adj a, double tol, int 
             d.DF[c] = 0.0f;
         }
     }
-    if (!grid_sum2(da, ra, pa, sh, last)) return;
+    if (!grid_sum2(da, ra, pa, sh, last, d.nblk_res)) return;
     if (threadIdx.x == 0) {
         const double resip = pa > 0.0 ? ra / pa : 0.0;
         a.pctl->resip = resip;

@@ -15,7 +15,11 @@
 namespace fvm {
 
 constexpr int WARP = 32;
-constexpr int RES_CELLS = 2;   // cells per thread of the Poisson residual kernels
+constexpr int RES_CELLS = 2;   // cells per thread of the mixed and adjoint Poisson residual kernels
+// cells per thread of the FP64 path's residual (k_pres64): eight amortise the block
+// reduction over more cells and leave room for the overlapping sweep launches (FP64
+// step 39.7 -> 35.7 ms on 512 x 384; two, for the mixed path's k_mres, measured best)
+constexpr int RES64_CELLS = 8;
 
 // One set of constant tridiagonal factors for a family of lines (one line per
 // radial row j, or per circumferential column i), solved by groups of NW warps
@@ -76,7 +80,8 @@ struct Dev {
     int dd_pos;         // 1: cell (i,j) takes the cross term of cell (i-1,j-1) in DIF / ITER_P
     int refine_sweeps;  // MIXED: FP32 sweeps per FP64 refinement
     int adi_refine;     // MIXED: defect-correction passes of a predictor line
-    int nblk_res;       // blocks of this case in the residual kernels
+    int nblk_res;       // blocks of this case in the residual kernels (RES_CELLS per thread)
+    int nblk_res64;     // blocks of this case in the FP64 path's residual (RES64_CELLS per thread)
     int case_id;        // position in a batch
     BatchCtl *bctl;     // batch control (nullptr in a single-context launch)
     fvm_coeffs *bhist;  // batch: coefficient records [step * ncases + case]
@@ -161,6 +166,7 @@ struct fvm_ctx {
     cudaGraphExec_t pgraph = nullptr;
     int pgraph_batch = 0;
     int nblk_res = 0;      // blocks of the residual kernels
+    int nblk_res64 = 0;    // blocks of the FP64 path's residual kernel
     // instrumentation
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;   // span around the first sweep group of a replay
     int pgraph_kernels = 0;                       // kernel nodes in the Poisson graph
@@ -215,7 +221,7 @@ struct Tgt {
     const Dev *one = nullptr;    // single context: its device view (passed by value)
     DevTable tab{nullptr};       // batch: device table of the cases' views
     int nz = 1;                  // cases
-    int NI = 0, NJ = 0, n = 0, nblk_res = 0;   // launch extents
+    int NI = 0, NJ = 0, n = 0, nblk_res = 0, nblk_res64 = 0;   // launch extents
     LineSys tr{}, tt{};          // tiles (NW, M) of the radial and circumferential line families
     int mixed = 0, thermal = 1, iter_t_bug = 1, refine_sweeps = 1, res_every = 2;
 };

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(256) k_mres(const __grid_constant__ S src, cud
         }
     }
     griddep_launch();
-    if (!grid_sum2(d, ra, pa, sh, last)) return;
+    if (!grid_sum2(d, ra, pa, sh, last, d.nblk_res)) return;
     if (threadIdx.x == 0) {
         double resip = ra / pa;
         d.pctl->resip = resip;

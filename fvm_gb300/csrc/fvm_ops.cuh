@@ -178,17 +178,17 @@ __device__ __forceinline__ void block_sum2(double &a, double &b, double *sh)
     }
 }
 
-// Publish a block's partial sums and, in the last block to arrive, reduce all
-// partials in a fixed order.  Returns true in the last block (sums in a, b on
+// Publish a block's partial sums and, in the last block to arrive (of nblk blocks),
+// reduce all partials in a fixed order.  Returns true in the last block (sums in a, b on
 // thread 0).
-__device__ __forceinline__ bool grid_sum2(const Dev &d, double &a, double &b, double *sh, bool &last)
+__device__ __forceinline__ bool grid_sum2(const Dev &d, double &a, double &b, double *sh, bool &last, int nblk)
 {
     block_sum2(a, b, sh);
     if (threadIdx.x == 0) {
         d.partial[2 * blockIdx.x] = a;
         d.partial[2 * blockIdx.x + 1] = b;
         __threadfence();
-        const unsigned nb = (unsigned)d.nblk_res;
+        const unsigned nb = (unsigned)nblk;
         unsigned t = atomicInc(&d.pctl->ticket, nb - 1);
         last = (t == nb - 1);
     }
@@ -197,7 +197,7 @@ __device__ __forceinline__ bool grid_sum2(const Dev &d, double &a, double &b, do
     __threadfence();
     a = 0.0;
     b = 0.0;
-    for (int k = threadIdx.x; k < d.nblk_res; k += blockDim.x) {
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
         a += ((volatile double *)d.partial)[2 * k];
         b += ((volatile double *)d.partial)[2 * k + 1];
     }

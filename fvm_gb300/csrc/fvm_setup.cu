@@ -169,6 +169,8 @@ int setup_allocate(fvm_ctx *c)
     const int interior = (c->NI - 1) * (c->NJ - 1);
     c->nblk_res = (interior + 256 * RES_CELLS - 1) / (256 * RES_CELLS);   // residual kernels
     d.nblk_res = c->nblk_res;
+    c->nblk_res64 = (interior + 256 * RES64_CELLS - 1) / (256 * RES64_CELLS);   // FP64 residual (fewer)
+    d.nblk_res64 = c->nblk_res64;
     Bump probe{nullptr};
     carve(probe, c, c->nblk_res);
     c->slab_bytes = probe.off + 256;

@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(256) k_pres64(const __grid_constant__ S src, c
     __shared__ double sh[64];
     __shared__ bool last;
     const Dev &d = dev_of(src);
-    if ((int)blockIdx.x >= d.nblk_res) return;   // beyond this case's blocks (batch)
+    if ((int)blockIdx.x >= d.nblk_res64) return;   // beyond this case's blocks (batch)
     griddep_wait();
     batch_body_guard<HAS_COND>(d, cond);
     if (d.pctl->done) return;
@@ -446,8 +446,8 @@ __global__ void __launch_bounds__(256) k_pres64(const __grid_constant__ S src, c
     const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
     double ra = 0.0, pa = 0.0;
 #pragma unroll
-    for (int q = 0; q < RES_CELLS; q++) {
-        int e = (blockIdx.x * RES_CELLS + q) * 256 + threadIdx.x;
+    for (int q = 0; q < RES64_CELLS; q++) {
+        int e = (blockIdx.x * RES64_CELLS + q) * 256 + threadIdx.x;
         if (e < total) {
             int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
             double su = d.DIVDT[c] - dd_src(d, d.P2, i, j);
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(256) k_pres64(const __grid_constant__ S src, c
         }
     }
     griddep_launch();
-    if (!grid_sum2(d, ra, pa, sh, last)) return;
+    if (!grid_sum2(d, ra, pa, sh, last, d.nblk_res64)) return;
     if (threadIdx.x == 0) {
         double resip = ra / pa;
         d.pctl->niter = it;
@@ -593,6 +593,7 @@ Tgt tgt_of(fvm_ctx *c)
     t.NJ = c->NJ;
     t.n = c->n;
     t.nblk_res = c->nblk_res;
+    t.nblk_res64 = c->nblk_res64;
     t.tr = c->d.sP;
     t.tt = c->d.sUY;
     t.mixed = c->p.precision == FVM_MIXED;
@@ -689,8 +690,8 @@ int poisson64_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond)
     }
     with_src(t, [&](const auto &src) {
         using S = std::decay_t<decltype(src)>;
-        if (has_cond) launch_pdl(k_pres64<1, S>, dim3(t.nblk_res, 1, t.nz), dim3(256), t.st, src, cond);
-        else launch_pdl(k_pres64<0, S>, dim3(t.nblk_res, 1, t.nz), dim3(256), t.st, src, cond);
+        if (has_cond) launch_pdl(k_pres64<1, S>, dim3(t.nblk_res64, 1, t.nz), dim3(256), t.st, src, cond);
+        else launch_pdl(k_pres64<0, S>, dim3(t.nblk_res64, 1, t.nz), dim3(256), t.st, src, cond);
     });
     KCOUNT(t.c);
     FVM_LAUNCH_CHECK(t.c);
