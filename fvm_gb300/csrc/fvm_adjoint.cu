@@ -747,6 +747,7 @@ __global__ void k_adj_pctl_reset(Adj a)
     a.pctl->niter = 0;
     a.pctl->done = 0;
     a.pctl->capped = 0;
+    a.pctl->fault = 0;
     a.pctl->resip = 0.0;
 }
 
@@ -1011,7 +1012,20 @@ int adj_poisson_graph(fvm_ctx *c)
     FVM_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const int blocks = line_blocks((c->NJ - 1) / 2, a.sPT.NW);
     bool ok = true;
-    for (int q = 0; q < groups && ok && mixed; q++) {
+    // the transposed FP32 correction: in the forward solve's resident kernel when the
+    // context uses it (its transposed factors share the forward tile), else per colour
+    const ResSys sys{a.sPT.invDf, a.sPT.faf, a.sPT.fbf, a.cPT.ANf, a.cPT.ASf, d.RF, d.DF, a.mu, a.pctl, 0};
+    for (int q = 0; q < groups && ok && mixed && c->res_lines; q++) {
+        k_adj_mres<<<c->nblk_res, 256, 0, c->stream>>>(d, a, c->p.resimax, c->d.nswpp);
+        int rc = resident_sweeps_on(c, sys, per, 1, 1);
+        if (rc) {
+            cudaGraph_t gg = nullptr;
+            cudaStreamEndCapture(c->stream, &gg);
+            if (gg) cudaGraphDestroy(gg);
+            return rc;
+        }
+    }
+    for (int q = 0; q < groups && ok && mixed && !c->res_lines; q++) {
         k_adj_mres<<<c->nblk_res, 256, 0, c->stream>>>(d, a, c->p.resimax, c->d.nswpp);
         for (int it = 0; it < per && ok; it++)
             for (int colour = 0; colour < 2; colour++)
@@ -1065,6 +1079,13 @@ int adj_poisson(fvm_ctx *c)
         if (A->h_pctl->done) break;
     }
     A->adj_sweeps += A->h_pctl->niter;
+    if (A->h_pctl->fault) {   // a bounded wait of the resident sweeps ran out
+        ARC(resident_reset(c));
+        FVM_CUDA(c, cudaMemsetAsync(&A->a.pctl->fault, 0, sizeof(int), c->stream));
+        FVM_CUDA(c, cudaStreamSynchronize(c->stream));
+        c->err = "adjoint Poisson: a bounded wait of the resident sweeps ran out";
+        return FVM_ERR_TIMEOUT;
+    }
     if (!std::isfinite(A->h_pctl->resip)) {
         c->err = "non-finite adjoint Poisson residual";
         return FVM_ERR_NAN;

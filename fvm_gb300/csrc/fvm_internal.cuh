@@ -277,8 +277,23 @@ int mixed_poisson_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_co
 int mixed_sweep_pair(const Tgt &t, int apply);
 int mixed_predictor_radial(const Tgt &t, int field, int colour, int refresh);
 int mixed_predictor_theta(const Tgt &t, int field, int colour, int ghosts);
-// line-resident FP32 sweeps (fvm_resident.cu)
+// line-resident FP32 sweeps (fvm_resident.cu).  The correction system a launch
+// solves: line factors (in the layout of the context's radial tile) and couplings,
+// the FP32 right-hand side and correction, the FP64 field the correction is added
+// to (bcp = 1: with the BCP ghost refresh of each updated row, the forward pressure;
+// 0: interior only) and the iteration's control block.
+struct ResSys {
+    const float *invDf, *faf, *fbf;
+    const float *ANf, *ASf;
+    const float *RF;
+    float *DF;
+    double *X;
+    PCtl *pctl;
+    int bcp;
+};
 int resident_setup(fvm_ctx *c);
+// the same launch on another system (the adjoint's transposed Poisson equation)
+int resident_sweeps_on(fvm_ctx *c, const ResSys &sys, int sweeps, int apply, int check_done);
 int resident_sweeps(const Tgt &t, int sweeps, int apply, int max_polls, unsigned tag_skew,
                     cudaGraphConditionalHandle cond, int has_cond, int check_done);
 int resident_reset(fvm_ctx *c);

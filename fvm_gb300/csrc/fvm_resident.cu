@@ -78,8 +78,8 @@ struct ResLayout {
 // afterwards.  check_done != 0 returns at once when the loop is already done.
 template <int M, int NW, int HAS_COND>
 __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
-    k_pois32_resident(const __grid_constant__ Dev d, int B, int S, int apply, int check_done, int max_polls,
-                      unsigned tag_skew, cudaGraphConditionalHandle cond)
+    k_pois32_resident(const __grid_constant__ Dev d, const __grid_constant__ ResSys sys, int B, int S, int apply,
+                      int check_done, int max_polls, unsigned tag_skew, cudaGraphConditionalHandle cond)
 {
     using Lay = ResLayout<M, NW>;
     constexpr int TG = Lay::TG, LW = Lay::LW;
@@ -96,23 +96,22 @@ __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
     const int n = d.sP.n;
     if (threadIdx.x == 0) {   // the loop's done flag, read once for the whole block
         s_fault = 0;
-        s_stop = check_done ? d.pctl->done : 0;
+        s_stop = check_done ? sys.pctl->done : 0;
     }
     __syncthreads();
     if (s_stop) return;
 
-    const LineSys &s = d.sP;
     const size_t base = size_t(j - 1) * LW;
     float fi[M], fa[M], fb[M], an[M], as[M], rf[M], v[M], halo[M];
-    load_factors<float, M, NW>(fi, fa, fb, s.invDf + base, s.faf + base, s.fbf + base, t);
+    load_factors<float, M, NW>(fi, fa, fb, sys.invDf + base, sys.faf + base, sys.fbf + base, t);
 #pragma unroll
     for (int k = 0; k < M; k++) {
         const int e = t * M + k;   // chunk ownership
         const bool ok = e < n;
         const int c = IDX(e + 1, j);
-        an[k] = ok ? d.cP.ANf[c] : 0.0f;
-        as[k] = ok ? d.cP.ASf[c] : 0.0f;
-        rf[k] = ok ? d.RF[c] : 0.0f;
+        an[k] = ok ? sys.ANf[c] : 0.0f;
+        as[k] = ok ? sys.ASf[c] : 0.0f;
+        rf[k] = ok ? sys.RF[c] : 0.0f;
         halo[k] = 0.0f;   // the correction starts from zero
         v[k] = 0.0f;
         lines[g * LW + k * TG + t] = 0.0f;
@@ -186,8 +185,8 @@ __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
 
     if (sw <= S) {   // a wait ran out: end the loop, leave P alone
         if (threadIdx.x == 0) {
-            d.pctl->fault = 1;
-            d.pctl->done = 1;
+            sys.pctl->fault = 1;
+            sys.pctl->done = 1;
             if (HAS_COND) cudaGraphSetConditional(cond, 0);
         }
         return;
@@ -196,24 +195,26 @@ __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
 #pragma unroll
         for (int k = 0; k < M; k++) {
             const int e = t * M + k;
-            if (e < n) d.DF[IDX(e + 1, j)] = v[k];
+            if (e < n) sys.DF[IDX(e + 1, j)] = v[k];
         }
         if (apply) {
 #pragma unroll
             for (int k = 0; k < M; k++) {
                 const int e = t * M + k;
-                if (e < n) d.P[IDX(e + 1, j)] += (double)v[k];
+                if (e < n) sys.X[IDX(e + 1, j)] += (double)v[k];
             }
-            bar();
-            if (t < WARP) refresh_row_ghosts<BCK_POISSON>(d, d.P, d.P, j, nullptr, nullptr, t);
+            if (sys.bcp) {
+                bar();
+                if (t < WARP) refresh_row_ghosts<BCK_POISSON>(d, sys.X, sys.X, j, nullptr, nullptr, t);
+            }
         }
     }
     if (threadIdx.x == 0) d.XCNT[blockIdx.x] = cnt0 + unsigned(S);
 }
 
 template <int M, int NW, int HAS_COND>
-cudaError_t launch_resident(const fvm_ctx *c, cudaStream_t st, int S, int apply, int check_done, int max_polls,
-                            unsigned skew, cudaGraphConditionalHandle cond)
+cudaError_t launch_resident(const fvm_ctx *c, const ResSys &sys, cudaStream_t st, int S, int apply, int check_done,
+                            int max_polls, unsigned skew, cudaGraphConditionalHandle cond)
 {
     using Lay = ResLayout<M, NW>;
     auto k = k_pois32_resident<M, NW, HAS_COND>;
@@ -228,7 +229,7 @@ cudaError_t launch_resident(const fvm_ctx *c, cudaStream_t st, int S, int apply,
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = c->res_coop ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k, c->d, c->res_lines, S, apply, check_done, max_polls, skew, cond);
+    return cudaLaunchKernelEx(&cfg, k, c->d, sys, c->res_lines, S, apply, check_done, max_polls, skew, cond);
 }
 
 }  // namespace
@@ -290,18 +291,24 @@ int resident_setup(fvm_ctx *c)
     return FVM_OK;
 }
 
-// One launch of the resident sweeps for a single context (batches use the
-// per-colour path).  max_polls <= 0 takes the default bound.
-int resident_sweeps(const Tgt &t, int sweeps, int apply, int max_polls, unsigned tag_skew,
-                    cudaGraphConditionalHandle cond, int has_cond, int check_done)
+namespace {
+
+// The forward pressure correction of a context.
+ResSys forward_sys(const fvm_ctx *c)
 {
-    fvm_ctx *c = t.c;
+    const Dev &d = c->d;
+    return ResSys{d.sP.invDf, d.sP.faf, d.sP.fbf, d.cP.ANf, d.cP.ASf, d.RF, d.DF, d.P, d.pctl, 1};
+}
+
+int launch_sys(fvm_ctx *c, const ResSys &sys, cudaStream_t st, int sweeps, int apply, int max_polls,
+               unsigned tag_skew, cudaGraphConditionalHandle cond, int has_cond, int check_done)
+{
     cudaError_t e = cudaErrorInvalidValue;
     const int polls = max_polls > 0 ? max_polls : kResidentPolls;
     bool ok = dispatch_line(c->d.sP, [&](auto m, auto nw) {
         constexpr int M_ = decltype(m)::value, NW_ = decltype(nw)::value;
-        if (has_cond) e = launch_resident<M_, NW_, 1>(c, t.st, sweeps, apply, check_done, polls, tag_skew, cond);
-        else e = launch_resident<M_, NW_, 0>(c, t.st, sweeps, apply, check_done, polls, tag_skew, cond);
+        if (has_cond) e = launch_resident<M_, NW_, 1>(c, sys, st, sweeps, apply, check_done, polls, tag_skew, cond);
+        else e = launch_resident<M_, NW_, 0>(c, sys, st, sweeps, apply, check_done, polls, tag_skew, cond);
     });
     if (!ok) {
         c->err = "line length above 512 cells is not supported";
@@ -313,6 +320,23 @@ int resident_sweeps(const Tgt &t, int sweeps, int apply, int max_polls, unsigned
     }
     KCOUNT(c);
     return FVM_OK;
+}
+
+}  // namespace
+
+// One launch of the resident sweeps for a single context (batches use the
+// per-colour path).  max_polls <= 0 takes the default bound.
+int resident_sweeps(const Tgt &t, int sweeps, int apply, int max_polls, unsigned tag_skew,
+                    cudaGraphConditionalHandle cond, int has_cond, int check_done)
+{
+    return launch_sys(t.c, forward_sys(t.c), t.st, sweeps, apply, max_polls, tag_skew, cond, has_cond, check_done);
+}
+
+// The same sweeps on another system of the context's line tile (the adjoint's
+// transposed Poisson equation); no graph condition, default wait bound.
+int resident_sweeps_on(fvm_ctx *c, const ResSys &sys, int sweeps, int apply, int check_done)
+{
+    return launch_sys(c, sys, c->stream, sweeps, apply, 0, 0u, 0, 0, check_done);
 }
 
 // After a wait ran out: the blocks' sweep counts may disagree, so clear the
