@@ -53,6 +53,10 @@ def case_inputs(w):
 # clocks during the timed region
 # ---------------------------------------------------------------------------------
 class ClockSampler:
+    """nvidia-smi every 100 ms in the background; only the samples that arrive
+    inside a timed window (begin() .. end(), several windows allowed) count.  open()
+    waits for the first sample, so that a short timed region does not start before
+    the sampler does."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -60,10 +64,11 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []
+        self.lines = []          # (arrival time, csv line)
+        self.windows = []
         self.t = None
 
-    def start(self):
+    def open(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
@@ -73,12 +78,30 @@ class ClockSampler:
             return
         self.t = threading.Thread(target=self._read, daemon=True)
         self.t.start()
+        t0 = time.monotonic()
+        while not self.lines and time.monotonic() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((time.monotonic(), ln.strip()))
+
+    def begin(self):
+        self.windows.append([time.monotonic(), None])
+
+    def end(self):
+        if self.windows and self.windows[-1][1] is None:
+            self.windows[-1][1] = time.monotonic()
+
+    def start(self):
+        self.open()
+        self.begin()
 
     def stop(self):
+        self.end()
+        return self.close()
+
+    def close(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -88,9 +111,10 @@ class ClockSampler:
             self.proc.kill()
         if self.t:
             self.t.join(timeout=2)
+        inside = [ln for t, ln in self.lines if any(a <= t <= b for a, b in self.windows if b is not None)]
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in inside:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -103,7 +127,8 @@ class ClockSampler:
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "timed_s": round(sum(b - a for a, b in self.windows if b is not None), 3)}
 
 
 # ---------------------------------------------------------------------------------
@@ -272,17 +297,19 @@ def run_ours(args):
     res = {}
     parts = {"all": (("mixed", capi.MIXED), ("fp64", capi.FP64)), "mixed": (("mixed", capi.MIXED),),
              "fp64": (("fp64", capi.FP64),)}[args.parts]
+    # one sampler over every timed region of this run (mixed, FP64, end to end)
+    clk = ClockSampler(local)
+    clk.open()
     for name, prec in parts:
         ctx = make_ctx(w, prec, local, g, du, dv)
         ext = torch.cuda.ExternalStream(ctx.stream_handle())
         ctx.step(args.warmup)
         ctx.timing_reset()
         dist.barrier()
-        clk = ClockSampler(local) if name == "mixed" else None
-        if clk:
-            clk.start()
+        clk.begin()
         ms = timed_steps(ctx, args.steps, flush, torch, ext)
-        clocks = clk.stop() if clk else None
+        clk.end()
+        clocks = None
         dist.barrier()
         ms_max = dist.max_over_ranks(ms, device="cuda")
         tm = ctx.timing()
@@ -298,6 +325,7 @@ def run_ours(args):
         ctx.close()
 
     if args.parts != "all":   # profiling runs: one path only
+        clk.close()
         nm = parts[0][0]
         if rank == 0:
             print(json.dumps({"metric": METRIC, "parts": nm, "ms_per_step": res[nm]["ms"] / args.steps,
@@ -314,6 +342,7 @@ def run_ours(args):
     ctx.download_ptrs(ptrs)
     e2e_ms = 0.0
     dist.barrier()
+    clk.begin()
     for _ in range(args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
@@ -326,6 +355,9 @@ def run_ours(args):
         b.record(ext)
         b.synchronize()
         e2e_ms += a.elapsed_time(b)
+    clk.end()
+    clocks = clk.close()
+    clocks["regions"] = "mixed, fp64 and e2e timed loops"
     dist.barrier()
     e2e_ms = dist.max_over_ranks(e2e_ms, device="cuda")
     ctx.close()
@@ -373,7 +405,7 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 7 * n * 8,
                 "d2h_bytes_per_step": 7 * n * 8 + 96},
         "gpu_launches": int(res["mixed"]["timing"]["kernel_launches"]),
-        "clocks": res["mixed"]["clocks"],
+        "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(w, g, du, dv)
@@ -673,6 +705,7 @@ def run_les3d_bench(args):
     ctx.download_ptrs(ptrs)
     e2e_ms = 0.0
     dist.barrier()
+    clk.begin()
     for _ in range(args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
@@ -685,6 +718,9 @@ def run_les3d_bench(args):
         b.record(ext)
         b.synchronize()
         e2e_ms += a.elapsed_time(b)
+    clk.end()
+    clocks = clk.close()
+    clocks["regions"] = "mixed, fp64 and e2e timed loops"
     dist.barrier()
     e2e_ms = dist.max_over_ranks(e2e_ms, device="cuda")
     ctx.close()
@@ -729,7 +765,7 @@ def run_les3d_bench(args):
         "roofline": roofline3d_with_traffic(n_int, res["mixed"]["sweep_ms"] / 2, peaks),
         "e2e": {"value": units / (e2e_ms * 1e-3) / 1e6, "unit": "Mcell-steps/s",
                 "h2d_bytes_per_step": len(FIELDS3D) * nbytes, "d2h_bytes_per_step": len(FIELDS3D) * nbytes},
-        "clocks": res["mixed"]["clocks"],
+        "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_3d(w, g, du, dv, dw, int(np.mean(res["fp64"]["sweeps"])))
