@@ -393,7 +393,8 @@ def run_ours(args):
                    "poisson": f"zebra line GS to scaled-L1 {w['resimax']:g}, cap NSWPP={w['nswpp']}",
                    "sweeps_per_step": res["mixed"]["sweeps"], "precision": "mixed: FP32 zebra sweeps in FP64 "
                    f"refinement every {w['refine_sweeps']} sweeps, FP32 predictor lines with 2 FP64 "
-                   "defect-correction passes; state, metrics and residuals FP64",
+                   "defect-correction passes; state and metrics FP64, Poisson residual in double-float "
+                   "(FP32 pairs) from the FP64 pressure",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "poisson_loop": POISSON_LOOP["mode"],
                    "l2": "256 MiB buffer written between timed steps (outside the events)"},

@@ -80,6 +80,7 @@ void make_target(fvm_batch *b)
         t.n = std::max(t.n, c->n);
         t.nblk_res = std::max(t.nblk_res, c->nblk_res);
         t.nblk_res64 = std::max(t.nblk_res64, c->nblk_res64);
+        t.nblk_mres = std::max(t.nblk_mres, c->nblk_mres);
     }
 }
 

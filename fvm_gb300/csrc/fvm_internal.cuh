@@ -20,6 +20,10 @@ constexpr int RES_CELLS = 2;   // cells per thread of the mixed and adjoint Pois
 // reduction over more cells and leave room for the overlapping sweep launches (FP64
 // step 39.7 -> 35.7 ms on 512 x 384; two, for the mixed path's k_mres, measured best)
 constexpr int RES64_CELLS = 8;
+// Tile of the mixed path's residual kernel k_mres: 32 radial x 8 circumferential
+// cells per 256-thread block, the pressure of the tile and its halo split into
+// double-float once in shared memory.
+constexpr int MRES_TI = 32, MRES_TJ = 8;
 
 // One set of constant tridiagonal factors for a family of lines (one line per
 // radial row j, or per circumferential column i), solved by groups of NW warps
@@ -82,6 +86,7 @@ struct Dev {
     int adi_refine;     // MIXED: defect-correction passes of a predictor line
     int nblk_res;       // blocks of this case in the residual kernels (RES_CELLS per thread)
     int nblk_res64;     // blocks of this case in the FP64 path's residual (RES64_CELLS per thread)
+    int nblk_mres;      // blocks of this case in the mixed path's residual (MRES_TI x MRES_TJ tiles)
     int case_id;        // position in a batch
     BatchCtl *bctl;     // batch control (nullptr in a single-context launch)
     fvm_coeffs *bhist;  // batch: coefficient records [step * ncases + case]
@@ -107,6 +112,9 @@ struct Dev {
     double *SU, *SUV, *SUT, *DD;   // per-field right-hand sides (U uses SU)
     // mixed-precision scratch
     float *RF, *DF;                // FP32 residual right-hand side and correction
+    // AE, AW, AN, AS, AP of the pressure equation and CNE, CSE, CNW, CSW, each split
+    // into double-float (hi, lo): nine planes of n cells for the mixed residual
+    float2 *PCD;
     // line-resident sweeps: boundary-line exchange words (value bits | tag << 32),
     // [slot 0/1][line][element], and each block's count of completed sweeps
     unsigned long long *XW;
@@ -167,6 +175,7 @@ struct fvm_ctx {
     int pgraph_batch = 0;
     int nblk_res = 0;      // blocks of the residual kernels
     int nblk_res64 = 0;    // blocks of the FP64 path's residual kernel
+    int nblk_mres = 0;     // blocks of the mixed path's residual kernel
     // instrumentation
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;   // span around the first sweep group of a replay
     int pgraph_kernels = 0;                       // kernel nodes in the Poisson graph
@@ -221,7 +230,7 @@ struct Tgt {
     const Dev *one = nullptr;    // single context: its device view (passed by value)
     DevTable tab{nullptr};       // batch: device table of the cases' views
     int nz = 1;                  // cases
-    int NI = 0, NJ = 0, n = 0, nblk_res = 0, nblk_res64 = 0;   // launch extents
+    int NI = 0, NJ = 0, n = 0, nblk_res = 0, nblk_res64 = 0, nblk_mres = 0;   // launch extents
     LineSys tr{}, tt{};          // tiles (NW, M) of the radial and circumferential line families
     int mixed = 0, thermal = 1, iter_t_bug = 1, refine_sweeps = 1, res_every = 2;
 };
@@ -237,6 +246,7 @@ Tgt tgt_of(fvm_ctx *c);
 int setup_allocate(fvm_ctx *c);
 void radial_tile(const fvm_ctx *c, int &nw, int &m);
 int setup_factors(fvm_ctx *c);
+void split_pcoef(fvm_ctx *c);   // double-float planes of the pressure coefficients (d.PCD)
 int setup_controls(fvm_ctx *c, double omega, const double *blow);
 int setup_grid(fvm_ctx *c);
 int setup_init(fvm_ctx *c, const double *du, const double *dv);

@@ -1,13 +1,14 @@
 // fvm_mixed.cu -- mixed-precision line solves: FP32 zebra sweeps and FP32 line
 // solves inside FP64 defect correction.
 //
-// Pressure Poisson (MIXED): each outer iteration forms in FP64 the full residual
-// r = SU - A P with SU = div/dt - DD(P) (iter_p.f90:24-30, 42-44) and its scaled
-// L1 norm (iter_p.f90:37-50); if not converged, refine_sweeps zebra line sweeps
-// solve A5 dP = r in FP32 from dP = 0 with the FP32 copies of the line factors,
-// and P += dP in FP64 with the BCP ghosts (bcp.f90:19-42) refreshed from the new P.
-// FP64 work per cell is one residual per refine_sweeps sweeps instead of a full
-// FP64 sweep each time; the fixed point is the FP64 solution.
+// Pressure Poisson (MIXED): each outer iteration forms the full residual
+// r = SU - A P with SU = div/dt - DD(P) (iter_p.f90:24-30, 42-44) of the FP64 P in
+// double-float (FP32 pairs, ~2^-46 relative per term) and its scaled L1 norm
+// (iter_p.f90:37-50); if not converged, refine_sweeps zebra line sweeps solve
+// A5 dP = r in FP32 from dP = 0 with the FP32 copies of the line factors, and
+// P += dP in FP64 with the BCP ghosts (bcp.f90:19-42) refreshed from the new P.
+// The fixed point is the FP64 solution to the residual's double-float rounding,
+// far below any Poisson tolerance; no FP64 sweep runs.
 //
 // Predictor lines (MIXED): the FP64 right-hand side C of a line (iter_u.f90:57-60)
 // is solved by adi_refine passes of  r = C - T x (FP64),  T dx = r (FP32),
@@ -16,39 +17,100 @@
 
 #include "fvm_internal.cuh"
 #include "fvm_ops.cuh"
+#include "fvm_df.cuh"
 
 namespace fvm {
 
-// FP64 residual of the current P, scaled-L1 norm, FP32 right-hand side of the
-// correction sweeps and zeroed correction.  The last block decides convergence.
+// The pressure-equation coefficients and cross-term weights split into
+// double-float planes for k_mres (dd_split: hi + lo within 2^-46 of the FP64 value).
+__global__ void k_pcoef_df(Dev d)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    const double *src[9] = {d.cP.AE, d.cP.AW, d.cP.AN, d.cP.AS, d.cP.AP, d.CNE, d.CSE, d.CNW, d.CSW};
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const dd v = dd_split(src[k][c]);
+        d.PCD[size_t(k) * d.n + c] = make_float2(v.hi, v.lo);
+    }
+}
+
+void split_pcoef(fvm_ctx *c)
+{
+    k_pcoef_df<<<(c->n + 255) / 256, 256, 0, c->stream>>>(c->d);
+}
+
+// Residual of the current P (iter_p.f90:24-30, 42-44: SU = DIVDT - DD(P), then the
+// five-point residual), its scaled-L1 norm (iter_p.f90:37-50), the FP32 right-hand
+// side of the correction sweeps and the zeroed correction.  The last block decides
+// convergence.
+//
+// Evaluated in double-float (the terms and order of dd_src and pres_at): about
+// 2^-46 relative to |AP P| per term, far below any Poisson tolerance, on the FP32
+// pipes instead of GB300's narrow FP64 pipe.  A block owns a tile of MRES_TI x
+// MRES_TJ cells; the pressure of the tile and of its halo (two cells below, one
+// above, in both directions: the positional cross term reaches (i-2, j-2)) is split
+// once into shared memory, the coefficients come pre-split (d.PCD), and the two
+// norms are summed in FP32 up to the warp and in FP64 beyond.
 template <int HAS_COND, class S>
 __global__ void __launch_bounds__(256) k_mres(const __grid_constant__ S src, cudaGraphConditionalHandle cond)
 {
+    constexpr int TI = MRES_TI, TJ = MRES_TJ, W = TI + 3, H = TJ + 3;
+    static_assert(TI == WARP && TI * TJ == 256, "one warp per tile row");
     __shared__ double sh[64];
     __shared__ bool last;
+    __shared__ float2 ps[H][W];
     const Dev &d = dev_of(src);
-    if ((int)blockIdx.x >= d.nblk_res) return;   // beyond this case's blocks (batch)
+    if ((int)blockIdx.x >= d.nblk_mres) return;   // beyond this case's blocks (batch)
     griddep_wait();
     batch_body_guard<HAS_COND>(d, cond);
     if (d.pctl->done) return;
     const int it = d.pctl->niter;
-    const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
-    double ra = 0.0, pa = 0.0;
-#pragma unroll
-    for (int q = 0; q < RES_CELLS; q++) {
-        int e = (blockIdx.x * RES_CELLS + q) * 256 + threadIdx.x;
-        if (e < total) {
-            int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
-            double su = d.DIVDT[c] - dd_src(d, d.P, i, j);
-            double r = pres_at(d, d.P, su, i, j);
-            ra += fabs(r);
-            pa += fabs(d.cP.AP[c] * d.P[c]);
-            d.RF[c] = (float)r;
-            d.DF[c] = 0.0f;
+    const int ti = (d.NI - 1 + TI - 1) / TI;
+    const int i0 = (blockIdx.x % ti) * TI + 1, j0 = (blockIdx.x / ti) * TJ + 1;   // first cell of the tile
+    const double *P = d.P;
+    for (int k = threadIdx.x; k < H * W; k += 256) {   // rows j0-2 .. j0+TJ, columns i0-2 .. i0+TI
+        const int r = k / W, q = k - r * W;
+        const int i = i0 - 2 + q, j = j0 - 2 + r;
+        dd v(0.0f, 0.0f);
+        if (i >= 0 && i <= d.NI && j >= 0 && j <= d.NJ) v = dd_split(P[IDX(i, j)]);
+        ps[r][q] = make_float2(v.hi, v.lo);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = i0 + tx, j = j0 + ty;
+    float raf = 0.0f, paf = 0.0f;
+    if (i <= d.NI - 1 && j <= d.NJ - 1) {
+        const int c = IDX(i, j);
+        auto at = [&](int a, int b) {   // P(i + a, j + b), rows as stored (ghost rows included)
+            const float2 v = ps[ty + 2 + b][tx + 2 + a];
+            return dd(v.x, v.y);
+        };
+        auto co = [&](int plane, int cc) {
+            const float2 v = d.PCD[size_t(plane) * d.n + cc];
+            return dd(v.x, v.y);
+        };
+        dd cross = dd(0.0f, 0.0f);   // dd_src: weights and neighbours of (i,j), or of (i-1,j-1)
+        if (!d.dd_pos) {
+            cross = ((co(5, c) * at(1, 1) + co(6, c) * at(1, -1)) + co(7, c) * at(-1, 1)) + co(8, c) * at(-1, -1);
+        } else if (i > 1 && j > 1) {
+            const int cc = IDX(i - 1, j - 1);
+            cross = ((co(5, cc) * at(0, 0) + co(6, cc) * at(0, -2)) + co(7, cc) * at(-2, 0)) + co(8, cc) * at(-2, -2);
         }
+        // circumferential neighbours through the periodic wrap (jwrap), as pres_at
+        const dd pn = (j + 1 == d.NJ) ? dd_split(P[IDX(i, 1)]) : at(0, 1);
+        const dd pso = (j == 1) ? dd_split(P[IDX(i, d.NJ - 1)]) : at(0, -1);
+        const dd su = dd_split(d.DIVDT[c]) - cross;
+        const dd app = co(4, c) * at(0, 0);
+        const dd r = ((((co(0, c) * at(1, 0) + co(1, c) * at(-1, 0)) + co(2, c) * pn) + co(3, c) * pso) + su) - app;
+        raf = fabsf(r.hi);
+        paf = fabsf(app.hi);
+        d.RF[c] = r.hi;
+        d.DF[c] = 0.0f;
     }
     griddep_launch();
-    if (!grid_sum2(d, ra, pa, sh, last, d.nblk_res)) return;
+    double ra, pa;
+    if (!grid_sum2f(d, raf, paf, ra, pa, sh, last, d.nblk_mres)) return;
     if (threadIdx.x == 0) {
         double resip = ra / pa;
         d.pctl->resip = resip;
@@ -162,15 +224,15 @@ int mixed_sweep_pair(const Tgt &t, int apply) { return sweep_pair(t, apply, 0); 
 // path the context's step uses (tests compare the two paths).
 int mixed_sweep_percolour(const Tgt &t, int apply) { return sweep_pair(t, apply, 0); }
 
-// One outer iteration of the MIXED Poisson: FP64 residual (ends the device-side
+// One outer iteration of the MIXED Poisson: residual (ends the device-side
 // loop when converged or capped), then refine_sweeps FP32 zebra sweeps, the last
 // of which adds the correction to P.
 int mixed_poisson_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond)
 {
     with_src(t, [&](const auto &src) {
         using S = std::decay_t<decltype(src)>;
-        if (has_cond) launch_pdl(k_mres<1, S>, dim3(t.nblk_res, 1, t.nz), dim3(256), t.st, src, cond);
-        else launch_pdl(k_mres<0, S>, dim3(t.nblk_res, 1, t.nz), dim3(256), t.st, src, cond);
+        if (has_cond) launch_pdl(k_mres<1, S>, dim3(t.nblk_mres, 1, t.nz), dim3(256), t.st, src, cond);
+        else launch_pdl(k_mres<0, S>, dim3(t.nblk_mres, 1, t.nz), dim3(256), t.st, src, cond);
     });
     KCOUNT(t.c);
     FVM_LAUNCH_CHECK(t.c);

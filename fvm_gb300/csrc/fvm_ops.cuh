@@ -157,13 +157,10 @@ __device__ __forceinline__ double dd_src(const Dev &d, const double *P, int i, i
     return (i > 1 && j > 1) ? dd_p(d, P, i - 1, j - 1) : 0.0;
 }
 
-// Deterministic block sum of two values (fixed shuffle tree, then warp 0).
-__device__ __forceinline__ void block_sum2(double &a, double &b, double *sh)
+// Cross-warp part of a block sum: lane 0 of every warp holds its warp's sums; warp 0
+// folds them in a fixed order (the block's sums end on thread 0).
+__device__ __forceinline__ void block_fold2(double &a, double &b, double *sh)
 {
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
-    }
     const int wid = threadIdx.x / WARP, lane = threadIdx.x & 31, nw = blockDim.x / WARP;
     __syncthreads();
     if (lane == 0) { sh[2 * wid] = a; sh[2 * wid + 1] = b; }
@@ -178,12 +175,21 @@ __device__ __forceinline__ void block_sum2(double &a, double &b, double *sh)
     }
 }
 
-// Publish a block's partial sums and, in the last block to arrive (of nblk blocks),
-// reduce all partials in a fixed order.  Returns true in the last block (sums in a, b on
-// thread 0).
-__device__ __forceinline__ bool grid_sum2(const Dev &d, double &a, double &b, double *sh, bool &last, int nblk)
+// Deterministic block sum of two values (fixed shuffle tree, then warp 0).
+__device__ __forceinline__ void block_sum2(double &a, double &b, double *sh)
 {
-    block_sum2(a, b, sh);
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    block_fold2(a, b, sh);
+}
+
+// Publish thread 0's block sums and, in the last block to arrive (of nblk blocks),
+// reduce all partials in a fixed order.  Returns true in the last block (sums in
+// a, b on thread 0).
+__device__ __forceinline__ bool grid_publish2(const Dev &d, double &a, double &b, double *sh, bool &last, int nblk)
+{
     if (threadIdx.x == 0) {
         d.partial[2 * blockIdx.x] = a;
         d.partial[2 * blockIdx.x + 1] = b;
@@ -203,6 +209,28 @@ __device__ __forceinline__ bool grid_sum2(const Dev &d, double &a, double &b, do
     }
     block_sum2(a, b, sh);
     return true;
+}
+
+// Grid sum of two FP64 values per thread (see grid_publish2).
+__device__ __forceinline__ bool grid_sum2(const Dev &d, double &a, double &b, double *sh, bool &last, int nblk)
+{
+    block_sum2(a, b, sh);
+    return grid_publish2(d, a, b, sh, last, nblk);
+}
+
+// Grid sum of two FP32 values per thread: summed in FP32 within the warp (fixed
+// tree), in FP64 from there on.  For norms that only need a few digits.
+__device__ __forceinline__ bool grid_sum2f(const Dev &d, float af, float bf, double &a, double &b, double *sh,
+                                           bool &last, int nblk)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        af += __shfl_down_sync(0xffffffffu, af, o);
+        bf += __shfl_down_sync(0xffffffffu, bf, o);
+    }
+    a = (double)af;
+    b = (double)bf;
+    block_fold2(a, b, sh);
+    return grid_publish2(d, a, b, sh, last, nblk);
 }
 
 // A case's Poisson iteration has ended (converged or capped).  Inside a batch the

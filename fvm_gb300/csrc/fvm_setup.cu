@@ -110,6 +110,7 @@ void carve(Bump &b, fvm_ctx *c, int nblk)
     for (auto p : st) *p = b.take<double>(n);
     d.RF = b.take<float>(n);
     d.DF = b.take<float>(n);
+    d.PCD = b.take<float2>(9 * n);
     // exchange words for the largest tile (32 x 4 warps x 4 elements per line)
     d.XW = b.take<unsigned long long>(2 * size_t(c->NJ - 1) * WARP * 4 * 4);
     d.XCNT = b.take<unsigned int>(size_t(c->NJ));
@@ -171,8 +172,11 @@ int setup_allocate(fvm_ctx *c)
     d.nblk_res = c->nblk_res;
     c->nblk_res64 = (interior + 256 * RES64_CELLS - 1) / (256 * RES64_CELLS);   // FP64 residual (fewer)
     d.nblk_res64 = c->nblk_res64;
+    c->nblk_mres = ((c->NI - 1 + MRES_TI - 1) / MRES_TI) * ((c->NJ - 1 + MRES_TJ - 1) / MRES_TJ);
+    d.nblk_mres = c->nblk_mres;
+    const int nblk_partial = std::max(c->nblk_res, c->nblk_mres);
     Bump probe{nullptr};
-    carve(probe, c, c->nblk_res);
+    carve(probe, c, nblk_partial);
     c->slab_bytes = probe.off + 256;
     cudaError_t e = cudaMalloc(&c->slab, c->slab_bytes);
     if (e != cudaSuccess) {
@@ -182,7 +186,7 @@ int setup_allocate(fvm_ctx *c)
     }
     FVM_CUDA(c, cudaMemsetAsync(c->slab, 0, c->slab_bytes, c->stream));
     Bump real{c->slab};
-    carve(real, c, c->nblk_res);
+    carve(real, c, nblk_partial);
     return FVM_OK;
 }
 
@@ -493,6 +497,7 @@ static int build_line_sets(fvm_ctx *c)
     Dev &d = c->d;
     dim3 blk(128), grd((c->NI - 1 + 127) / 128, c->NJ - 1);
     k_coef_p<<<grd, blk, 0, c->stream>>>(d, d.cP);
+    split_pcoef(c);
     k_coef_af<<<grd, blk, 0, c->stream>>>(d, d.cUX, d.XIX, d.ETX, d.re);
     k_coef_af<<<grd, blk, 0, c->stream>>>(d, d.cUY, d.XIY, d.ETY, d.re);
     k_coef_af<<<grd, blk, 0, c->stream>>>(d, d.cTX, d.XIX, d.ETX, d.pe);

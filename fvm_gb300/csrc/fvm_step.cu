@@ -594,6 +594,7 @@ Tgt tgt_of(fvm_ctx *c)
     t.n = c->n;
     t.nblk_res = c->nblk_res;
     t.nblk_res64 = c->nblk_res64;
+    t.nblk_mres = c->nblk_mres;
     t.tr = c->d.sP;
     t.tt = c->d.sUY;
     t.mixed = c->p.precision == FVM_MIXED;
