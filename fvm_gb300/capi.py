@@ -46,7 +46,7 @@ class Params(ctypes.Structure):
                 ("dd_positional", ctypes.c_int),
                 ("tile_r_warps", ctypes.c_int), ("tile_r_m", ctypes.c_int),
                 ("tile_t_warps", ctypes.c_int), ("tile_t_m", ctypes.c_int),
-                ("poisson_resident", ctypes.c_int)]
+                ("poisson_resident", ctypes.c_int), ("resident_depth", ctypes.c_int)]
 
 
 class Coeffs(ctypes.Structure):

@@ -49,6 +49,10 @@ int check_params(const fvm_params *p, std::string &why)
         why = "poisson_resident: 0, 1 or an even number of lines per block";
         return FVM_ERR_ARG;
     }
+    if (p->resident_depth < 0 || p->resident_depth > 2) {
+        why = "resident_depth: 0 (automatic), 1 or 2 sweeps per exchange";
+        return FVM_ERR_ARG;
+    }
     return FVM_OK;
 }
 

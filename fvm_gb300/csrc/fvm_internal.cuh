@@ -186,6 +186,7 @@ struct fvm_ctx {
     // line-resident Poisson sweeps (mixed path): lines per block (0: per-colour
     // launches), blocks, and whether the launch carries the cooperative attribute
     int res_lines = 0, res_blocks = 0;
+    int res_depth = 1;   // sweeps per boundary-line exchange (1, or 2 with 4 lines per block)
     bool res_coop = false;
     fvm::PostState post;
     int post_suspend = 0;   // recomputation passes of the adjoint: no post-processing

@@ -212,6 +212,181 @@ __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
     if (threadIdx.x == 0) d.XCNT[blockIdx.x] = cnt0 + unsigned(S);
 }
 
+// Two sweeps per exchange.  A block of B = 4 lines j0 .. j0+3 keeps the window of
+// lines j0-3 .. j0+B+3 on chip (rows w = 0 .. B+6, line j0-3+w; odd lines are the
+// odd rows) and solves rows 1 .. B+5, one line group each.  A pair of sweeps starts
+// from the previous sweep's values of the window's even lines; in the pair's first
+// sweep the odd rows 1 .. B+5 and then the even rows 2 .. B+4 are solved, in the
+// second the odd rows 3 .. B+3 and the even rows 4 .. B+2 (the block's own even
+// lines): each half-sweep needs both neighbours, so the valid part of the window
+// narrows by one row per half.  The rows beyond the block's own are the
+// neighbours' lines solved again here with the same inputs and code, so their bits
+// equal the owners'.  The only data from other blocks are the window's outer even
+// rows 0, 2 and B+4, B+6, which are the even lines of the blocks before and after:
+// every block publishes its two even lines once per pair and polls four lines at
+// the start of the next, so one exchange serves two sweeps.  Tags and slots as in
+// k_pois32_resident, counted per pair.
+template <int M, int NW>
+struct ResLayout2 {
+    static constexpr int B = 4;
+    static constexpr int TG = WARP * NW;
+    static constexpr int LW = TG * M;
+    static constexpr int NL = B + 7;   // window rows
+    static constexpr int NG = B + 5;   // line groups (rows 1 .. B+5)
+    static constexpr int NT = NG * TG;
+    static size_t bytes() { return sizeof(float) * (size_t(NL) * LW + size_t(NG) * 2 * NW); }
+};
+
+template <int M, int NW, int HAS_COND>
+__global__ void __launch_bounds__(ResLayout2<M, NW>::NT, 1)
+    k_pois32_resident2(const __grid_constant__ Dev d, const __grid_constant__ ResSys sys, int S, int apply,
+                       int check_done, int max_polls, unsigned tag_skew, cudaGraphConditionalHandle cond)
+{
+    using Lay = ResLayout2<M, NW>;
+    constexpr int TG = Lay::TG, LW = Lay::LW, B = Lay::B, NL = Lay::NL;
+    extern __shared__ float shm[];
+    __shared__ int s_fault, s_stop;
+    float *rows = shm;
+    const int gi = threadIdx.x / TG, t = threadIdx.x % TG;
+    const int w = gi + 1;   // the window row this group solves
+    float *xch = shm + size_t(NL) * LW + size_t(gi) * 2 * NW;
+    const NamedSync<NW> bar{1 + gi};
+    const int L = d.NJ - 1;
+    const int j0 = blockIdx.x * B + 1;
+    auto wrap = [L](int j) { return j < 1 ? j + L : (j > L ? j - L : j); };
+    const int j = wrap(j0 - 3 + w);
+    const int n = d.sP.n;
+    if (threadIdx.x == 0) {
+        s_fault = 0;
+        s_stop = check_done ? sys.pctl->done : 0;
+    }
+    __syncthreads();
+    if (s_stop) return;
+
+    const size_t base = size_t(j - 1) * LW;
+    float fi[M], fa[M], fb[M], an[M], as[M], rf[M], v[M];
+    load_factors<float, M, NW>(fi, fa, fb, sys.invDf + base, sys.faf + base, sys.fbf + base, t);
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        const int e = t * M + k;
+        const bool ok = e < n;
+        const int c = IDX(e + 1, j);
+        an[k] = ok ? sys.ANf[c] : 0.0f;
+        as[k] = ok ? sys.ASf[c] : 0.0f;
+        rf[k] = ok ? sys.RF[c] : 0.0f;
+        v[k] = 0.0f;
+    }
+    for (int q = threadIdx.x; q < NL * LW; q += Lay::NT) rows[q] = 0.0f;   // the correction starts from zero
+    const unsigned cnt0 = d.XCNT[blockIdx.x];
+    const bool odd = (w & 1) != 0;
+    // the outer even rows, each polled by the group next to it
+    const int hrow = w == 1 ? 0 : (w == 3 ? 2 : (w == B + 3 ? B + 4 : (w == B + 5 ? B + 6 : -1)));
+    const int hline = hrow >= 0 ? wrap(j0 - 3 + hrow) : 0;
+    const bool publish = !odd && w >= 4 && w <= B + 2;
+    __syncthreads();
+
+    auto solve = [&]() {
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            const float xs = rows[(w - 1) * LW + k * TG + t];
+            const float xn = rows[(w + 1) * LW + k * TG + t];
+            v[k] = t * M + k < n ? pois32_rhs(an[k], xn, as[k], xs, rf[k]) : 0.0f;
+        }
+        group_apply_r<float, M, NW>(v, fi, fa, fb, t, xch, bar);
+#pragma unroll
+        for (int k = 0; k < M; k++) rows[w * LW + k * TG + t] = v[k];
+    };
+
+    int sw = 1;
+    for (; sw <= S; sw += 2) {   // sweeps sw and sw+1
+        if (sw > 1 && hrow >= 0) {
+            const unsigned want = cnt0 + unsigned(sw - 1) + tag_skew;
+            const unsigned long long *src = d.XW + (size_t(((sw - 1) >> 1) & 1) * L + (hline - 1)) * LW;
+            unsigned pending = 0;
+#pragma unroll
+            for (int k = 0; k < M; k++)
+                if (t * M + k < n) pending |= 1u << k;
+            for (int it = 0; pending && it < max_polls; it++) {
+                unsigned long long wd[M];
+#pragma unroll
+                for (int k = 0; k < M; k++) wd[k] = ((pending >> k) & 1u) ? ld_word(src + k * TG + t) : 0ull;
+#pragma unroll
+                for (int k = 0; k < M; k++) {
+                    if (((pending >> k) & 1u) && unsigned(wd[k] >> 32) == want) {
+                        rows[hrow * LW + k * TG + t] = __uint_as_float(unsigned(wd[k]));
+                        pending &= ~(1u << k);
+                    }
+                }
+            }
+            if (pending) s_fault = 1;
+        }
+        __syncthreads();
+        if (s_fault) break;   // uniform: read by every thread after the barrier
+        if (odd) solve();                                  // sweep sw, odd rows 1 .. B+5
+        __syncthreads();
+        if (!odd) solve();                                 // sweep sw, even rows 2 .. B+4
+        __syncthreads();
+        if (odd && w >= 3 && w <= B + 3) solve();          // sweep sw+1, odd rows 3 .. B+3
+        __syncthreads();
+        if (publish) {                                     // sweep sw+1, the block's even lines
+            solve();
+            unsigned long long *dst = d.XW + (size_t(((sw + 1) >> 1) & 1) * L + (j - 1)) * LW;
+            const unsigned long long tag = (unsigned long long)(cnt0 + unsigned(sw + 1)) << 32;
+#pragma unroll
+            for (int k = 0; k < M; k++)
+                if (t * M + k < n) st_word(dst + k * TG + t, tag | __float_as_uint(v[k]));
+        }
+        __syncthreads();
+    }
+
+    if (sw <= S) {   // a wait ran out: end the loop, leave P alone
+        if (threadIdx.x == 0) {
+            sys.pctl->fault = 1;
+            sys.pctl->done = 1;
+            if (HAS_COND) cudaGraphSetConditional(cond, 0);
+        }
+        return;
+    }
+    if (w >= 3 && w <= B + 2) {   // the block's own lines
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            const int e = t * M + k;
+            if (e < n) sys.DF[IDX(e + 1, j)] = v[k];
+        }
+        if (apply) {
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const int e = t * M + k;
+                if (e < n) sys.X[IDX(e + 1, j)] += (double)v[k];
+            }
+            if (sys.bcp) {
+                bar();
+                if (t < WARP) refresh_row_ghosts<BCK_POISSON>(d, sys.X, sys.X, j, nullptr, nullptr, t);
+            }
+        }
+    }
+    if (threadIdx.x == 0) d.XCNT[blockIdx.x] = cnt0 + unsigned(S);
+}
+
+template <int M, int NW, int HAS_COND>
+cudaError_t launch_resident2(const fvm_ctx *c, const ResSys &sys, cudaStream_t st, int S, int apply, int check_done,
+                             int max_polls, unsigned skew, cudaGraphConditionalHandle cond)
+{
+    using Lay = ResLayout2<M, NW>;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c->res_blocks);
+    cfg.blockDim = dim3(Lay::NT);
+    cfg.dynamicSmemBytes = Lay::bytes();
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = c->res_coop ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_pois32_resident2<M, NW, HAS_COND>, c->d, sys, S, apply, check_done, max_polls,
+                              skew, cond);
+}
+
 template <int M, int NW, int HAS_COND>
 cudaError_t launch_resident(const fvm_ctx *c, const ResSys &sys, cudaStream_t st, int S, int apply, int check_done,
                             int max_polls, unsigned skew, cudaGraphConditionalHandle cond)
@@ -288,6 +463,32 @@ int resident_setup(fvm_ctx *c)
         c->err = "poisson_resident: the requested lines per block do not divide NJ-1 into co-resident blocks";
         return FVM_ERR_ARG;
     }
+    // two sweeps per exchange where the window fits: 4 lines per block, line groups
+    // of one or two warps, at least three blocks around the ring, all co-resident
+    c->res_depth = 1;
+    if (c->res_lines == 4 && c->p.resident_depth != 1 && c->res_blocks >= 3) {
+        cudaError_t e = cudaSuccess;
+        dispatch_line(s, [&](auto m, auto nw) {
+            constexpr int M_ = decltype(m)::value, NW_ = decltype(nw)::value;
+            if constexpr (NW_ <= 2) {
+                using Lay = ResLayout2<M_, NW_>;
+                auto k0 = k_pois32_resident2<M_, NW_, 0>;
+                auto k1 = k_pois32_resident2<M_, NW_, 1>;
+                int per_sm = 0;
+                e = cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::bytes());
+                if (e == cudaSuccess)
+                    e = cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::bytes());
+                if (e == cudaSuccess)
+                    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k1, Lay::NT, Lay::bytes());
+                if (e == cudaSuccess && c->res_blocks <= per_sm * sms) c->res_depth = 2;
+            }
+        });
+        if (e != cudaSuccess) cudaGetLastError();
+    }
+    if (c->p.resident_depth == 2 && c->res_depth != 2) {
+        c->err = "resident_depth 2: needs 4 lines per block, line groups of at most two warps and 12 or more lines";
+        return FVM_ERR_ARG;
+    }
     return FVM_OK;
 }
 
@@ -305,8 +506,16 @@ int launch_sys(fvm_ctx *c, const ResSys &sys, cudaStream_t st, int sweeps, int a
 {
     cudaError_t e = cudaErrorInvalidValue;
     const int polls = max_polls > 0 ? max_polls : kResidentPolls;
+    const bool pairs = c->res_depth == 2 && sweeps % 2 == 0;   // two sweeps per exchange
     bool ok = dispatch_line(c->d.sP, [&](auto m, auto nw) {
         constexpr int M_ = decltype(m)::value, NW_ = decltype(nw)::value;
+        if constexpr (NW_ <= 2) {
+            if (pairs) {
+                if (has_cond) e = launch_resident2<M_, NW_, 1>(c, sys, st, sweeps, apply, check_done, polls, tag_skew, cond);
+                else e = launch_resident2<M_, NW_, 0>(c, sys, st, sweeps, apply, check_done, polls, tag_skew, cond);
+                return;
+            }
+        }
         if (has_cond) e = launch_resident<M_, NW_, 1>(c, sys, st, sweeps, apply, check_done, polls, tag_skew, cond);
         else e = launch_resident<M_, NW_, 0>(c, sys, st, sweeps, apply, check_done, polls, tag_skew, cond);
     });

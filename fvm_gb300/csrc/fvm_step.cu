@@ -1053,7 +1053,8 @@ int run_resident_wait_test(fvm_ctx *c, int max_polls)
         c->err = "the context does not use the resident sweep path";
         return FVM_ERR_ARG;
     }
-    RC(resident_sweeps(tgt_of(c), 2, 0, max_polls, 0x40000000u, 0, 0, 0));
+    // four sweeps: waits at sweeps 2-4 (one exchange per sweep) or at sweep 3 (per pair)
+    RC(resident_sweeps(tgt_of(c), 4, 0, max_polls, 0x40000000u, 0, 0, 0));
     FVM_CUDA(c, cudaMemcpyAsync(c->h_pctl, c->d.pctl, sizeof(PCtl), cudaMemcpyDeviceToHost, c->stream));
     FVM_CUDA(c, cudaStreamSynchronize(c->stream));
     if (!c->h_pctl->fault) {

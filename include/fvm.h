@@ -76,6 +76,12 @@ typedef struct fvm_params {
        lines (1, the default: lines per block chosen automatically; k >= 2, even:
        k lines per block; 0: one launch per zebra colour).  Same results bit for bit. */
     int poisson_resident;
+    /* Resident sweeps: sweeps per exchange of boundary lines between blocks (0, the
+       default: 2 where the layout allows it -- 4 lines per block, line groups of one
+       or two warps, NJ-1 >= 12 -- else 1; 1; 2: required).  Two sweeps per exchange
+       solve three more lines per block redundantly and halve the exchanges.  Same
+       results bit for bit. */
+    int resident_depth;
 } fvm_params;
 
 /* Per-step diagnostics of CALCCOEF (calccoef.f90:9-120) plus Poisson statistics. */
