@@ -62,47 +62,56 @@ __global__ void __launch_bounds__(256) k_mres(const __grid_constant__ S src, cud
     __shared__ float2 ps[H][W];
     const Dev &d = dev_of(src);
     if ((int)blockIdx.x >= d.nblk_mres) return;   // beyond this case's blocks (batch)
+    const int ti = (d.NI - 1 + TI - 1) / TI;
+    const int i0 = (blockIdx.x % ti) * TI + 1, j0 = (blockIdx.x / ti) * TJ + 1;   // first cell of the tile
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = i0 + tx, j = j0 + ty;
+    const bool inside = i <= d.NI - 1 && j <= d.NJ - 1;
+    // dd_src: the weights of (i,j), or of (i-1,j-1) (zero on row/column 1)
+    const bool has_cross = inside && (!d.dd_pos || (i > 1 && j > 1));
+    const int c = inside ? IDX(i, j) : 0;
+    const int cc = d.dd_pos ? (has_cross ? IDX(i - 1, j - 1) : 0) : c;
+    // the coefficient planes are written at set-up only: loaded before the wait for
+    // the preceding kernel
+    float2 cf[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const bool ok = k < 5 ? inside : has_cross;
+        cf[k] = ok ? d.PCD[size_t(k) * d.n + (k < 5 ? c : cc)] : make_float2(0.0f, 0.0f);
+    }
     griddep_wait();
     batch_body_guard<HAS_COND>(d, cond);
     if (d.pctl->done) return;
     const int it = d.pctl->niter;
-    const int ti = (d.NI - 1 + TI - 1) / TI;
-    const int i0 = (blockIdx.x % ti) * TI + 1, j0 = (blockIdx.x / ti) * TJ + 1;   // first cell of the tile
     const double *P = d.P;
+    const double divdt = inside ? d.DIVDT[c] : 0.0;
     for (int k = threadIdx.x; k < H * W; k += 256) {   // rows j0-2 .. j0+TJ, columns i0-2 .. i0+TI
         const int r = k / W, q = k - r * W;
-        const int i = i0 - 2 + q, j = j0 - 2 + r;
+        const int ih = i0 - 2 + q, jh = j0 - 2 + r;
         dd v(0.0f, 0.0f);
-        if (i >= 0 && i <= d.NI && j >= 0 && j <= d.NJ) v = dd_split(P[IDX(i, j)]);
+        if (ih >= 0 && ih <= d.NI && jh >= 0 && jh <= d.NJ) v = dd_split(P[IDX(ih, jh)]);
         ps[r][q] = make_float2(v.hi, v.lo);
     }
     __syncthreads();
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int i = i0 + tx, j = j0 + ty;
     float raf = 0.0f, paf = 0.0f;
-    if (i <= d.NI - 1 && j <= d.NJ - 1) {
-        const int c = IDX(i, j);
+    if (inside) {
         auto at = [&](int a, int b) {   // P(i + a, j + b), rows as stored (ghost rows included)
             const float2 v = ps[ty + 2 + b][tx + 2 + a];
             return dd(v.x, v.y);
         };
-        auto co = [&](int plane, int cc) {
-            const float2 v = d.PCD[size_t(plane) * d.n + cc];
-            return dd(v.x, v.y);
-        };
-        dd cross = dd(0.0f, 0.0f);   // dd_src: weights and neighbours of (i,j), or of (i-1,j-1)
+        auto co = [&](int k) { return dd(cf[k].x, cf[k].y); };
+        dd cross = dd(0.0f, 0.0f);
         if (!d.dd_pos) {
-            cross = ((co(5, c) * at(1, 1) + co(6, c) * at(1, -1)) + co(7, c) * at(-1, 1)) + co(8, c) * at(-1, -1);
-        } else if (i > 1 && j > 1) {
-            const int cc = IDX(i - 1, j - 1);
-            cross = ((co(5, cc) * at(0, 0) + co(6, cc) * at(0, -2)) + co(7, cc) * at(-2, 0)) + co(8, cc) * at(-2, -2);
+            cross = ((co(5) * at(1, 1) + co(6) * at(1, -1)) + co(7) * at(-1, 1)) + co(8) * at(-1, -1);
+        } else if (has_cross) {
+            cross = ((co(5) * at(0, 0) + co(6) * at(0, -2)) + co(7) * at(-2, 0)) + co(8) * at(-2, -2);
         }
         // circumferential neighbours through the periodic wrap (jwrap), as pres_at
         const dd pn = (j + 1 == d.NJ) ? dd_split(P[IDX(i, 1)]) : at(0, 1);
         const dd pso = (j == 1) ? dd_split(P[IDX(i, d.NJ - 1)]) : at(0, -1);
-        const dd su = dd_split(d.DIVDT[c]) - cross;
-        const dd app = co(4, c) * at(0, 0);
-        const dd r = ((((co(0, c) * at(1, 0) + co(1, c) * at(-1, 0)) + co(2, c) * pn) + co(3, c) * pso) + su) - app;
+        const dd su = dd_split(divdt) - cross;
+        const dd app = co(4) * at(0, 0);
+        const dd r = ((((co(0) * at(1, 0) + co(1) * at(-1, 0)) + co(2) * pn) + co(3) * pso) + su) - app;
         raf = fabsf(r.hi);
         paf = fabsf(app.hi);
         d.RF[c] = r.hi;
