@@ -201,11 +201,25 @@ __device__ __forceinline__ bool grid_publish2(const Dev &d, double &a, double &b
     __syncthreads();
     if (!last) return false;
     __threadfence();
+    // partial k in thread k mod blockDim, in increasing k; four loads in flight per
+    // thread (L2 only: the partials were written by other SMs)
     a = 0.0;
     b = 0.0;
-    for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
-        a += ((volatile double *)d.partial)[2 * k];
-        b += ((volatile double *)d.partial)[2 * k + 1];
+    const double2 *pp = reinterpret_cast<const double2 *>(d.partial);
+    for (int k0 = threadIdx.x; k0 < nblk; k0 += 4 * blockDim.x) {
+        double2 x[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int k = k0 + r * (int)blockDim.x;
+            x[r] = k < nblk ? __ldcg(pp + k) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            if (k0 + r * (int)blockDim.x < nblk) {
+                a += x[r].x;
+                b += x[r].y;
+            }
+        }
     }
     block_sum2(a, b, sh);
     return true;
