@@ -53,7 +53,7 @@ void split_pcoef(fvm_ctx *c)
 // once into shared memory, the coefficients come pre-split (d.PCD), and the two
 // norms are summed in FP32 up to the warp and in FP64 beyond.
 template <int HAS_COND, class S>
-__global__ void __launch_bounds__(256) k_mres(const __grid_constant__ S src, cudaGraphConditionalHandle cond)
+__global__ void __launch_bounds__(256, 6) k_mres(const __grid_constant__ S src, cudaGraphConditionalHandle cond)
 {
     constexpr int TI = MRES_TI, TJ = MRES_TJ, W = TI + 3, H = TJ + 3;
     static_assert(TI == WARP && TI * TJ == 256, "one warp per tile row");
