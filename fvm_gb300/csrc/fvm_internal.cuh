@@ -60,7 +60,7 @@ struct PCtl {
     int fault;          // 1 if a bounded wait of the resident sweep kernel ran out
     double resip;       // last scaled residual
     unsigned int ticket;
-    unsigned int pad2;
+    unsigned int xbase;   // resident path: the blocks' sweep count (XCNT) when the step's Poisson loop began
     double pad3;
 };
 
@@ -301,12 +301,15 @@ struct ResSys {
     double *X;
     PCtl *pctl;
     int bcp;
+    // 1: the launch first sums the block partials the forward residual kernel left
+    // and takes the loop's convergence decision (forward Poisson loop only)
+    int decide;
 };
 int resident_setup(fvm_ctx *c);
 // the same launch on another system (the adjoint's transposed Poisson equation)
 int resident_sweeps_on(fvm_ctx *c, const ResSys &sys, int sweeps, int apply, int check_done);
 int resident_sweeps(const Tgt &t, int sweeps, int apply, int max_polls, unsigned tag_skew,
-                    cudaGraphConditionalHandle cond, int has_cond, int check_done);
+                    cudaGraphConditionalHandle cond, int has_cond, int check_done, int decide = 0);
 int resident_reset(fvm_ctx *c);
 }  // namespace fvm
 

@@ -51,8 +51,10 @@ void split_pcoef(fvm_ctx *c)
 // MRES_TJ cells; the pressure of the tile and of its halo (two cells below, one
 // above, in both directions: the positional cross term reaches (i-2, j-2)) is split
 // once into shared memory, the coefficients come pre-split (d.PCD), and the two
-// norms are summed in FP32 up to the warp and in FP64 beyond.
-template <int HAS_COND, class S>
+// norms are summed in FP32 up to the warp and in FP64 beyond.  DECIDE = 0 (the
+// single-context resident path) leaves the block sums in d.partial for the resident
+// sweep launch to decide convergence (resident_decide); DECIDE = 1 decides here.
+template <int HAS_COND, class S, int DECIDE>
 __global__ void __launch_bounds__(256, 6) k_mres(const __grid_constant__ S src, cudaGraphConditionalHandle cond)
 {
     constexpr int TI = MRES_TI, TJ = MRES_TJ, W = TI + 3, H = TJ + 3;
@@ -119,6 +121,14 @@ __global__ void __launch_bounds__(256, 6) k_mres(const __grid_constant__ S src, 
     }
     griddep_launch();
     double ra, pa;
+    if (!DECIDE) {
+        block_sum2f(raf, paf, ra, pa, sh);
+        if (threadIdx.x == 0) {
+            d.partial[2 * blockIdx.x] = ra;
+            d.partial[2 * blockIdx.x + 1] = pa;
+        }
+        return;
+    }
     if (!grid_sum2f(d, raf, paf, ra, pa, sh, last, d.nblk_mres)) return;
     if (threadIdx.x == 0) {
         double resip = ra / pa;
@@ -238,15 +248,19 @@ int mixed_sweep_percolour(const Tgt &t, int apply) { return sweep_pair(t, apply,
 // of which adds the correction to P.
 int mixed_poisson_body(const Tgt &t, cudaGraphConditionalHandle cond, int has_cond)
 {
+    // one context with resident sweeps: the interval in one resident launch, which
+    // also takes the convergence decision from the residual's block sums
+    const bool resident = !t.tab.devs && t.c->res_lines;
     with_src(t, [&](const auto &src) {
         using S = std::decay_t<decltype(src)>;
-        if (has_cond) launch_pdl(k_mres<1, S>, dim3(t.nblk_mres, 1, t.nz), dim3(256), t.st, src, cond);
-        else launch_pdl(k_mres<0, S>, dim3(t.nblk_mres, 1, t.nz), dim3(256), t.st, src, cond);
+        const dim3 g(t.nblk_mres, 1, t.nz);
+        if (resident) launch_pdl(k_mres<0, S, 0>, g, dim3(256), t.st, src, cond);
+        else if (has_cond) launch_pdl(k_mres<1, S, 1>, g, dim3(256), t.st, src, cond);
+        else launch_pdl(k_mres<0, S, 1>, g, dim3(256), t.st, src, cond);
     });
     KCOUNT(t.c);
     FVM_LAUNCH_CHECK(t.c);
-    if (!t.tab.devs && t.c->res_lines)   // one context: the interval in one resident launch
-        return resident_sweeps(t, t.refine_sweeps, 1, 0, 0u, cond, has_cond, 1);
+    if (resident) return resident_sweeps(t, t.refine_sweeps, 1, 0, 0u, cond, has_cond, 1, 1);
     for (int s = 0; s < t.refine_sweeps; s++) {
         int rc = sweep_pair(t, s == t.refine_sweeps - 1, 1);
         if (rc) return rc;

@@ -232,10 +232,10 @@ __device__ __forceinline__ bool grid_sum2(const Dev &d, double &a, double &b, do
     return grid_publish2(d, a, b, sh, last, nblk);
 }
 
-// Grid sum of two FP32 values per thread: summed in FP32 within the warp (fixed
-// tree), in FP64 from there on.  For norms that only need a few digits.
-__device__ __forceinline__ bool grid_sum2f(const Dev &d, float af, float bf, double &a, double &b, double *sh,
-                                           bool &last, int nblk)
+// Block sum of two FP32 values per thread: summed in FP32 within the warp (fixed
+// tree), in FP64 from there on (sums on thread 0).  For norms that only need a few
+// digits.
+__device__ __forceinline__ void block_sum2f(float af, float bf, double &a, double &b, double *sh)
 {
     for (int o = 16; o > 0; o >>= 1) {
         af += __shfl_down_sync(0xffffffffu, af, o);
@@ -244,7 +244,44 @@ __device__ __forceinline__ bool grid_sum2f(const Dev &d, float af, float bf, dou
     a = (double)af;
     b = (double)bf;
     block_fold2(a, b, sh);
+}
+
+// Grid sum of two FP32 values per thread (block_sum2f, then grid_publish2).
+__device__ __forceinline__ bool grid_sum2f(const Dev &d, float af, float bf, double &a, double &b, double *sh,
+                                           bool &last, int nblk)
+{
+    block_sum2f(af, bf, a, b, sh);
     return grid_publish2(d, a, b, sh, last, nblk);
+}
+
+// The sums grid_publish2's last block forms, formed by any block of at least 256
+// threads from partials another kernel left: thread k < 256 adds partials k, k+256,
+// ... in increasing order, threads from 256 on contribute zero (which leaves the
+// shuffle trees' sums unchanged), then block_sum2.  Same bits as grid_publish2 with
+// 256-thread blocks.
+__device__ __forceinline__ void sum_partials256(const double *partial, int nblk, double &a, double &b, double *sh)
+{
+    a = 0.0;
+    b = 0.0;
+    if (threadIdx.x < 256) {
+        const double2 *pp = reinterpret_cast<const double2 *>(partial);
+        for (int k0 = threadIdx.x; k0 < nblk; k0 += 4 * 256) {
+            double2 x[4];
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int k = k0 + r * 256;
+                x[r] = k < nblk ? __ldcg(pp + k) : make_double2(0.0, 0.0);
+            }
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                if (k0 + r * 256 < nblk) {
+                    a += x[r].x;
+                    b += x[r].y;
+                }
+            }
+        }
+    }
+    block_sum2(a, b, sh);
 }
 
 // A case's Poisson iteration has ended (converged or capped).  Inside a batch the

@@ -55,6 +55,38 @@ __device__ __forceinline__ void st_word(unsigned long long *p, unsigned long lon
     asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Convergence decision of the forward Poisson loop at the start of a resident
+// launch (sys.decide): every block sums the block partials the residual kernel
+// k_mres left, in that kernel's own order (the same bits in every block), and takes
+// k_mres's decision (iter_p.f90:37-50: done once the scaled residual is at the
+// tolerance or the sweeps reach the cap) with the loop's sweep count from its own
+// XCNT; block 0 records it.  Returns true when the loop is done: the launch then
+// does nothing.  This takes the last-block reduction off the residual kernel's
+// critical path.
+template <int HAS_COND>
+__device__ bool resident_decide(const Dev &d, const ResSys &sys, int S, double *sh, cudaGraphConditionalHandle cond)
+{
+    double a, b;
+    sum_partials256(d.partial, d.nblk_mres, a, b, sh);
+    if (threadIdx.x == 0) sh[0] = a / b;   // warp 0 has finished reading sh
+    __syncthreads();
+    const double resip = sh[0];
+    const int it = (int)(d.XCNT[blockIdx.x] - sys.pctl->xbase);
+    const bool stop = it > 0 && !(resip > d.resimax && it < d.nswpp);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sys.pctl->resip = resip;
+        if (stop) {
+            sys.pctl->done = 1;
+            sys.pctl->capped = (resip > d.resimax) ? 1 : 0;
+            sys.pctl->niter = it;
+            if (HAS_COND) cudaGraphSetConditional(cond, 0);
+        } else {
+            sys.pctl->niter = it + S;
+        }
+    }
+    return stop;
+}
+
 // Shared memory of a block: the block's current line values (B+1 lines, LW words
 // each) and one fold buffer per line group.  Every value of the block stays in the
 // chunk ownership of the line solve (thread t of a group holds elements
@@ -85,6 +117,7 @@ __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
     constexpr int TG = Lay::TG, LW = Lay::LW;
     extern __shared__ float shm[];
     __shared__ int s_fault, s_stop;
+    __shared__ double s_sum[64];
     float *lines = shm;
     const int g = threadIdx.x / TG, t = threadIdx.x % TG;
     float *xch = shm + size_t(B + 1) * LW + size_t(g) * 2 * NW;
@@ -100,6 +133,7 @@ __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
     }
     __syncthreads();
     if (s_stop) return;
+    if (sys.decide && resident_decide<HAS_COND>(d, sys, S, s_sum, cond)) return;
 
     const size_t base = size_t(j - 1) * LW;
     float fi[M], fa[M], fb[M], an[M], as[M], rf[M], v[M], halo[M];
@@ -246,6 +280,7 @@ __global__ void __launch_bounds__(ResLayout2<M, NW>::NT, 1)
     constexpr int TG = Lay::TG, LW = Lay::LW, B = Lay::B, NL = Lay::NL;
     extern __shared__ float shm[];
     __shared__ int s_fault, s_stop;
+    __shared__ double s_sum[64];
     float *rows = shm;
     const int gi = threadIdx.x / TG, t = threadIdx.x % TG;
     const int w = gi + 1;   // the window row this group solves
@@ -262,6 +297,7 @@ __global__ void __launch_bounds__(ResLayout2<M, NW>::NT, 1)
     }
     __syncthreads();
     if (s_stop) return;
+    if (sys.decide && resident_decide<HAS_COND>(d, sys, S, s_sum, cond)) return;
 
     const size_t base = size_t(j - 1) * LW;
     float fi[M], fa[M], fb[M], an[M], as[M], rf[M], v[M];
@@ -498,7 +534,7 @@ namespace {
 ResSys forward_sys(const fvm_ctx *c)
 {
     const Dev &d = c->d;
-    return ResSys{d.sP.invDf, d.sP.faf, d.sP.fbf, d.cP.ANf, d.cP.ASf, d.RF, d.DF, d.P, d.pctl, 1};
+    return ResSys{d.sP.invDf, d.sP.faf, d.sP.fbf, d.cP.ANf, d.cP.ASf, d.RF, d.DF, d.P, d.pctl, 1, 0};
 }
 
 int launch_sys(fvm_ctx *c, const ResSys &sys, cudaStream_t st, int sweeps, int apply, int max_polls,
@@ -536,9 +572,11 @@ int launch_sys(fvm_ctx *c, const ResSys &sys, cudaStream_t st, int sweeps, int a
 // One launch of the resident sweeps for a single context (batches use the
 // per-colour path).  max_polls <= 0 takes the default bound.
 int resident_sweeps(const Tgt &t, int sweeps, int apply, int max_polls, unsigned tag_skew,
-                    cudaGraphConditionalHandle cond, int has_cond, int check_done)
+                    cudaGraphConditionalHandle cond, int has_cond, int check_done, int decide)
 {
-    return launch_sys(t.c, forward_sys(t.c), t.st, sweeps, apply, max_polls, tag_skew, cond, has_cond, check_done);
+    ResSys sys = forward_sys(t.c);
+    sys.decide = decide;
+    return launch_sys(t.c, sys, t.st, sweeps, apply, max_polls, tag_skew, cond, has_cond, check_done);
 }
 
 // The same sweeps on another system of the context's line tile (the adjoint's

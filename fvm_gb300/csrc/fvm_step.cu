@@ -84,6 +84,7 @@ __global__ void k_contra_vel(const __grid_constant__ S src, int with_poisson)
             d.pctl->done = 0;
             d.pctl->capped = 0;
             d.pctl->resip = 0.0;
+            d.pctl->xbase = d.XCNT[0];
             if (d.bctl && d.case_id == 0) {
                 d.bctl->remaining = d.bctl->ncases;
                 d.bctl->bodies = 0;
