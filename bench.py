@@ -229,7 +229,7 @@ def vs_oracle(res, ofields, oco, w):
     return out
 
 
-def roofline_sweep(w, ms_per_colour, peaks, mixed, resident=False):
+def roofline_sweep(w, ms_per_colour, peaks, mixed, resident=False, layout=None):
     """Roofline of the Poisson sweep kernel from its measured time per zebra colour.
     Algorithmic bytes per colour (half the cells active):
     FP32 sweep: per active cell RF, ANf, ASf, invDf, faf, fbf read and DF written
@@ -255,11 +255,15 @@ def roofline_sweep(w, ms_per_colour, peaks, mixed, resident=False):
            "avg_launch_us": ms_per_colour * 1e3, "bytes_per_launch": per_colour, "peak_source": peak_src}
     if resident:
         spl = w["refine_sweeps"]
-        out.update({"kernel": "k_pois32_resident", "sweeps_per_launch": spl,
+        pairs = bool(layout) and layout.get("sweeps_per_exchange") == 2
+        out.update({"kernel": "k_pois32_resident2" if pairs else "k_pois32_resident", "sweeps_per_launch": spl,
                     "avg_launch_us": 2 * ms_per_colour * 1e3 * spl, "bytes_per_launch": 2 * per_colour * spl,
                     "per_sweep_us": 2 * ms_per_colour * 1e3, "bytes_per_sweep": 2 * per_colour,
                     "note": "lines' factors, couplings, right-hand side and correction stay on chip for the "
-                            "interval; one launch per refine_sweeps sweeps"})
+                            "interval; one launch per refine_sweeps sweeps" +
+                            ("; boundary lines exchanged once per two sweeps (three lines per block solved "
+                             "again)" if pairs else ""),
+                    "layout": layout})
     return out
 
 
@@ -321,7 +325,7 @@ def run_ours(args):
         fields = {nm: ctx.get(nm).copy() for nm in ("U", "V", "P", "T")}
         res[name] = dict(ms=ms_max, timing=tm, clocks=clocks, sweeps=hist[0]["sweeps"], fields=fields,
                          cd=hist[0]["cd"], cl=hist[0]["cl"], nu=hist[0]["nu"], resid=hist[0]["resid"],
-                         sweep_ms=sweep_ms, resident=(sweep_launches == 1))
+                         sweep_ms=sweep_ms, resident=(sweep_launches == 1), layout=ctx.resident_info())
         ctx.close()
 
     if args.parts != "all":   # profiling runs: one path only
@@ -370,14 +374,14 @@ def run_ours(args):
     value = units / (res["mixed"]["ms"] * 1e-3) / 1e6
     fp64_value = units / (res["fp64"]["ms"] * 1e-3) / 1e6
     e2e_value = units / (e2e_ms * 1e-3) / 1e6
-    roof = roofline_sweep(w, res["mixed"]["sweep_ms"], peaks, True, res["mixed"]["resident"])
+    roof = roofline_sweep(w, res["mixed"]["sweep_ms"], peaks, True, res["mixed"]["resident"],
+                          res["mixed"]["layout"])
     roof64 = roofline_sweep(w, res["fp64"]["sweep_ms"], peaks, False)
     if roof64:
         roof64["fp64_issue"] = fp64_pipe("fp64_pipe_cylinder2d_512x384", "k_pois64")
         roof64["fp64_issue_residual"] = fp64_pipe("fp64_pipe_cylinder2d_512x384", "k_pres64")
-    traffic_file = os.path.join(ROOT, "profiles", ("k_pois32_resident_cylinder2d_512x384.json"
-                                                   if res["mixed"]["resident"] else
-                                                   "k_pois32_cylinder2d_512x384.json"))
+    traffic_file = os.path.join(ROOT, "profiles", (roof["kernel"] if roof else "k_pois32") +
+                                "_cylinder2d_512x384.json")
     if roof and os.path.exists(traffic_file):
         try:
             roof["traffic"] = json.load(open(traffic_file)).get("dram_bytes_per_launch")

@@ -27,6 +27,7 @@ EXPORTS = ["fvm_default_params", "fvm_create", "fvm_destroy", "fvm_last_error", 
            "fvm_iter_u", "fvm_iter_v", "fvm_remove_grad", "fvm_iter_p", "fvm_correct", "fvm_iter_t",
            "fvm_calccoef", "fvm_step", "fvm_history", "fvm_synchronize", "fvm_get_stream",
            "fvm_timing_reset", "fvm_get_timing", "fvm_time_sweeps", "fvm_resident_wait_test",
+           "fvm_resident_info",
            "fvm_poisson_residual_static",
            "fvm_batch_create", "fvm_batch_destroy", "fvm_batch_last_error", "fvm_batch_case",
            "fvm_batch_tiles", "fvm_batch_set_tiles", "fvm_batch_autotune", "fvm_batch_time_sweeps",
@@ -135,6 +136,7 @@ def load(build_if_missing: bool = True):
     L.fvm_get_timing.argtypes = [V, ctypes.POINTER(Timing)]
     L.fvm_time_sweeps.argtypes = [V, ctypes.c_int, D, ctypes.POINTER(ctypes.c_longlong)]
     L.fvm_resident_wait_test.argtypes = [V, ctypes.c_int]
+    L.fvm_resident_info.argtypes = [V] + [ctypes.POINTER(ctypes.c_int)] * 3
     L.fvm_poisson_residual_static.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 8 + [V]
     I = ctypes.POINTER(ctypes.c_int)
     L.fvm_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(Params), ctypes.POINTER(V)]
@@ -349,6 +351,13 @@ class Context:
         """fvm_resident_wait_test: status code (FVM_ERR_TIMEOUT when the bounded
         waits of the resident sweeps reported running out)."""
         return self.L.fvm_resident_wait_test(self.h, max_polls)
+
+    def resident_info(self) -> dict:
+        """fvm_resident_info: lines per block (0: per-colour path), blocks and sweeps
+        per boundary-line exchange of the resident Poisson sweeps."""
+        v = [ctypes.c_int() for _ in range(3)]
+        self._ok(self.L.fvm_resident_info(self.h, *[ctypes.byref(x) for x in v]))
+        return {"lines_per_block": v[0].value, "blocks": v[1].value, "sweeps_per_exchange": v[2].value}
 
     def timing(self) -> dict:
         t = Timing()

@@ -336,6 +336,16 @@ int fvm_resident_wait_test(fvm_ctx *c, int max_polls)
     return fvm::run_resident_wait_test(c, max_polls);
 }
 
+int fvm_resident_info(fvm_ctx *c, int *lines_per_block, int *blocks, int *sweeps_per_exchange)
+{
+    READY();
+    if (!lines_per_block || !blocks || !sweeps_per_exchange) return bad(c, "null output pointer");
+    *lines_per_block = c->res_lines;
+    *blocks = c->res_blocks;
+    *sweeps_per_exchange = c->res_lines ? c->res_depth : 0;
+    return FVM_OK;
+}
+
 }  // extern "C"
 
 namespace fvm {

@@ -224,12 +224,15 @@ int fvm_get_timing(struct fvm_ctx *ctx, fvm_timing *out);
  * is its time divided by 2*sweeps). */
 int fvm_time_sweeps(struct fvm_ctx *ctx, int sweeps, double *ms_per_launch, long long *launches);
 /* Check of the bounded waits of the resident sweeps (MIXED contexts using them):
- * two sweeps on scratch arrays with exchange tags that no block publishes, so
+ * four sweeps on scratch arrays with exchange tags that no block publishes, so
  * every wait for a neighbouring block runs out after max_polls polls (1 .. 2^24).
  * Returns FVM_ERR_TIMEOUT when the kernel reported it, as a step would; the
  * state is unchanged and the exchange state cleared, so the context stays usable.
  * FVM_ERR_ARG if the context does not use the resident path. */
 int fvm_resident_wait_test(struct fvm_ctx *ctx, int max_polls);
+/* Layout of the resident Poisson sweeps the context chose: lines per block (0: the
+ * per-colour path), blocks, and sweeps per exchange of boundary lines (1 or 2). */
+int fvm_resident_info(struct fvm_ctx *ctx, int *lines_per_block, int *blocks, int *sweeps_per_exchange);
 
 /* Allocation-free scaled residual of the pressure equation.  No counterpart in
  * the reference: it serves callers that cannot allocate device memory (code
