@@ -29,6 +29,7 @@
 
 #include "fvm_internal.cuh"
 #include "fvm_ops.cuh"
+#include "fvm_df.cuh"
 
 namespace fvm {
 
@@ -64,9 +65,9 @@ __device__ void wall_normal(const Dev &d, int j, double &DN1, double &TH2)
     const int c = IDX(1, j);
     const double X = d.X[c], Y = d.Y[c];
     const double xa = d.XG[IDX(1, j)], ya = d.YG[IDX(1, j)], xb = d.XG[IDX(1, j + 1)], yb = d.YG[IDX(1, j + 1)];
-    double L1 = sqrt((X - xa) * (X - xa) + (Y - ya) * (Y - ya));
-    double L2 = sqrt((X - xb) * (X - xb) + (Y - yb) * (Y - yb));
-    double L3 = sqrt((xb - xa) * (xb - xa) + (yb - ya) * (yb - ya));
+    double L1 = ::sqrt((X - xa) * (X - xa) + (Y - ya) * (Y - ya));
+    double L2 = ::sqrt((X - xb) * (X - xb) + (Y - yb) * (Y - yb));
+    double L3 = ::sqrt((xb - xa) * (xb - xa) + (yb - ya) * (yb - ya));
     double TH1 = acos((((L1 * L1) + (L2 * L2)) - (L3 * L3)) / ((2.0 * L1) * L2));
     DN1 = ((L1 * L2) / L3) * sin(TH1);
     double LA = (yb - ya) / (xb - xa);
@@ -75,7 +76,7 @@ __device__ void wall_normal(const Dev &d, int j, double &DN1, double &TH2)
     double LB_ = Y - LA_ * X;
     double X1 = (LB_ - LB) / (LA - LA_);
     double Y1 = (LA * (LB_ - LB)) / (LA - LA_) + LB;
-    double DN2 = sqrt((Y - Y1) * (Y - Y1) + (X - X1) * (X - X1));
+    double DN2 = ::sqrt((Y - Y1) * (Y - Y1) + (X - X1) * (X - X1));
     TH2 = atan((Y - Y1) / (X - X1));
     double sg = asin((Y - Y1) / DN2);
     if (TH2 >= 0.0 && sg > 0.0) TH2 = TH2;
@@ -558,6 +559,48 @@ __device__ __forceinline__ double xd_at(const Dev &d, const double *mu, int i, i
     return s;
 }
 
+// qdd and xd_at in double-float (the same terms in the same order, each FP64
+// operand split on load): the mixed path's residual of the transposed equation.
+__device__ __forceinline__ dd qdd_df(const Dev &d, const double *mu, int x, int y)
+{
+    const int o = d.dd_pos;
+    dd q(0.0f, 0.0f);
+    auto term = [&](const double *C, int a, int b) {
+        const int i = a + o, j = b + o;
+        if (a < 1 || b < 1 || i > d.NI - 1 || j > d.NJ - 1) return;
+        q = q + dd_split(C[IDX(a, b)]) * dd_split(mu[IDX(i, j)]);
+    };
+    term(d.CNE, x - 1, y - 1);
+    term(d.CSE, x - 1, y + 1);
+    term(d.CNW, x + 1, y - 1);
+    term(d.CSW, x + 1, y + 1);
+    return q;
+}
+
+__device__ __forceinline__ dd xd_at_df(const Dev &d, const double *mu, int i, int j)
+{
+    const int NI = d.NI, NJ = d.NJ;
+    dd s = qdd_df(d, mu, i, j);
+    if (j == NJ - 1) s = s + qdd_df(d, mu, i, 0);
+    if (j == 1) s = s + qdd_df(d, mu, i, NJ);
+    if (i == 1) {
+        s = s + qdd_df(d, mu, 0, j);
+        if (j == NJ - 1) s = s + qdd_df(d, mu, 0, 0);
+        if (j == 1) s = s + qdd_df(d, mu, 0, NJ);
+    }
+    float w = 0.0f;
+    if (i == NI - 1) w += 3.0f;
+    if (i == NI - 2) w -= 3.0f;
+    if (i == NI - 3) w += 1.0f;
+    if (w != 0.0f) {
+        dd g = qdd_df(d, mu, NI, j);
+        if (j == NJ - 1) g = g + qdd_df(d, mu, NI, 0);
+        if (j == 1) g = g + qdd_df(d, mu, NI, NJ);
+        s = s + dd(w, 0.0f) * g;
+    }
+    return s;
+}
+
 __global__ void k_adj_xd(Dev d, Adj a)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
@@ -642,11 +685,12 @@ __global__ void __launch_bounds__(256) k_adj_pres(Dev d, Adj a, int per, double 
     }
 }
 
-// MIXED: the transposed Poisson equation by FP64 defect correction around FP32 zebra
-// sweeps, as the forward solve.  Each outer iteration forms in FP64 the residual
-// r = g - XD(mu) - A^T mu with the cross term of the current mu, its scaled L1 norm
-// (the convergence test) and r in FP32; refine_sweeps FP32 zebra sweeps solve
-// A^T dmu = r from dmu = 0; mu += dmu in FP64.
+// MIXED: the transposed Poisson equation by defect correction of the FP64 mu around
+// FP32 zebra sweeps, as the forward solve.  Each outer iteration forms the residual
+// r = g - XD(mu) - A^T mu with the cross term of the current mu in double-float
+// (FP32 pairs, ~2^-46 relative per term, as the forward residual), its scaled L1
+// norm (the convergence test; FP32 within a warp, FP64 beyond) and r in FP32;
+// refine_sweeps FP32 zebra sweeps solve A^T dmu = r from dmu = 0; mu += dmu in FP64.
 __global__ void __launch_bounds__(256) k_adj_mres(Dev d, Adj a, double tol, int nmax)
 {
     __shared__ double sh[64];
@@ -658,23 +702,27 @@ __global__ void __launch_bounds__(256) k_adj_mres(Dev d, Adj a, double tol, int 
     const int it = a.pctl->niter;
     const int ni1 = d.NI - 1, total = ni1 * (d.NJ - 1);
     const Coef &cf = a.cPT;
-    double ra = 0.0, pa = 0.0;
+    float raf = 0.0f, paf = 0.0f;
 #pragma unroll
     for (int q = 0; q < RES_CELLS; q++) {
         int e = (blockIdx.x * RES_CELLS + q) * 256 + threadIdx.x;
         if (e < total) {
             int i = e % ni1 + 1, j = e / ni1 + 1, c = IDX(i, j);
             const double *mu = a.mu;
-            double am = cf.AP[c] * mu[c] - cf.AE[c] * mu[IDX(i + 1, j)] - cf.AW[c] * mu[IDX(i - 1, j)] -
-                        cf.AN[c] * mu[IDX(i, jwrap(d, j + 1))] - cf.AS[c] * mu[IDX(i, jwrap(d, j - 1))];
-            double r = (a.g[c] - xd_at(d, mu, i, j)) - am;
-            ra += fabs(r);
-            pa += fabs(cf.AP[c] * mu[c]);
-            d.RF[c] = (float)r;
+            const dd app = dd_split(cf.AP[c]) * dd_split(mu[c]);
+            const dd am = (((app - dd_split(cf.AE[c]) * dd_split(mu[IDX(i + 1, j)])) -
+                            dd_split(cf.AW[c]) * dd_split(mu[IDX(i - 1, j)])) -
+                           dd_split(cf.AN[c]) * dd_split(mu[IDX(i, jwrap(d, j + 1))])) -
+                          dd_split(cf.AS[c]) * dd_split(mu[IDX(i, jwrap(d, j - 1))]);
+            const dd r = (dd_split(a.g[c]) - xd_at_df(d, mu, i, j)) - am;
+            raf += fabsf(r.hi);
+            paf += fabsf(app.hi);
+            d.RF[c] = r.hi;
             d.DF[c] = 0.0f;
         }
     }
-    if (!grid_sum2(da, ra, pa, sh, last, d.nblk_res)) return;
+    double ra, pa;
+    if (!grid_sum2f(da, raf, paf, ra, pa, sh, last, d.nblk_res)) return;
     if (threadIdx.x == 0) {
         const double resip = pa > 0.0 ? ra / pa : 0.0;
         a.pctl->resip = resip;
