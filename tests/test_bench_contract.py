@@ -48,3 +48,45 @@ def test_3d_default_params():
     p = capi3d.default_params()
     assert (p.ni, p.nj, p.nk) == (241, 201, 121) and p.nswpp == 20 and p.resimax == 1e-4
     assert p.precision == capi.FP64 and p.poisson_host_loop == 1 and p.tile_i_warps == 0
+
+
+def test_resident_roofline_names_the_kernel_it_timed():
+    w = dict(bench.WORKLOAD)
+    spl = w["refine_sweeps"]
+    two = bench.roofline_sweep(w, 0.7e-3, {"hbm_gbs": 6790.0}, True, True,
+                               {"lines_per_block": 4, "blocks": 128, "sweeps_per_exchange": 2})
+    one = bench.roofline_sweep(w, 0.8e-3, {"hbm_gbs": 6790.0}, True, True,
+                               {"lines_per_block": 4, "blocks": 128, "sweeps_per_exchange": 1})
+    assert two["kernel"] == "k_pois32_resident2" and one["kernel"] == "k_pois32_resident"
+    assert two["per_sweep_us"] == pytest.approx(1.4) and two["sweeps_per_launch"] == spl
+    assert two["bytes_per_sweep"] == 32.0 * bench.cells(w)
+    assert two["avg_launch_us"] == pytest.approx(1.4 * spl)
+
+
+def test_clock_sampler_counts_only_readings_inside_timed_windows(tmp_path, monkeypatch):
+    """A stand-in nvidia-smi prints a reading every 50 ms, SM clock 1000 MHz outside
+    and 2070 inside the two windows the test opens; only the latter may count."""
+    flag = tmp_path / "inside"
+    fake = tmp_path / "nvidia-smi"
+    fake.write_text("#!/bin/sh\nwhile true; do\n  if [ -e '%s' ]; then c=2070; r='Active'; else c=1000; r='Not Active'; fi\n"
+                    "  echo \"0, $c, 2070, 500.0, 0x0, Not Active, Not Active, Not Active, $r\"\n"
+                    "  sleep 0.05\ndone\n" % flag)
+    fake.chmod(0o755)
+    monkeypatch.setenv("PATH", str(tmp_path) + os.pathsep + os.environ.get("PATH", ""))
+    import time
+    clk = bench.ClockSampler(0)
+    clk.open()
+    time.sleep(0.3)
+    for _ in range(2):
+        flag.write_text("1")
+        time.sleep(0.15)
+        clk.begin()
+        time.sleep(0.5)
+        clk.end()
+        flag.unlink()
+        time.sleep(0.4)
+    out = clk.close()
+    assert out["samples"] >= 8
+    assert out["sm_mhz"] == 2070.0 and out["sm_max_mhz"] == 2070.0
+    assert out["reasons"] == ["sw_power_cap"]
+    assert out["timed_s"] == pytest.approx(1.0, abs=0.1)
