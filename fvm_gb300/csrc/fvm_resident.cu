@@ -33,6 +33,11 @@
 // added to P in FP64 with the BCP ghosts refreshed) is the per-colour kernel's,
 // operation for operation, so both paths give identical bits.  Compiled with
 // -ftz=true, as the per-colour sweeps are.
+//
+// k_pois32_resident2 (below) exchanges once per two sweeps: 4-line blocks keep an
+// 11-line window and solve the neighbours' three nearest lines again; and either
+// kernel, launched inside the forward Poisson loop, first takes the loop's
+// convergence decision from the residual kernel's block sums (resident_decide).
 #include <type_traits>
 
 #include "fvm_internal.cuh"
