@@ -222,6 +222,9 @@ __global__ void __launch_bounds__(ResLayout<M, NW>::MAXT, 1)
         __syncthreads();
     }
 
+    // the next residual launch (programmatic) may start its coefficient prologue;
+    // it reads P only after its dependency wait, i.e. after this grid has finished
+    griddep_launch();
     if (sw <= S) {   // a wait ran out: end the loop, leave P alone
         if (threadIdx.x == 0) {
             sys.pctl->fault = 1;
@@ -380,6 +383,9 @@ __global__ void __launch_bounds__(ResLayout2<M, NW>::NT, 1)
         __syncthreads();
     }
 
+    // the next residual launch (programmatic) may start its coefficient prologue;
+    // it reads P only after its dependency wait, i.e. after this grid has finished
+    griddep_launch();
     if (sw <= S) {   // a wait ran out: end the loop, leave P alone
         if (threadIdx.x == 0) {
             sys.pctl->fault = 1;
